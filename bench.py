@@ -1,0 +1,347 @@
+"""Benchmark of the fv2d residual-and-update step on one GB300.
+
+Workload (default): 2-D Navier-Stokes flow around a circular cylinder (D = 1, centred in a
+40 x 20 box) on a ~1M-cell polygonal Voronoi mesh with jittered seeds graded from 0.005 at the
+wall to 0.1 far away; Re = 100, Mach 0.2, Pr = 0.72, NO_SLIP_WALL cylinder, FREESTREAM box,
+second order with the squeeze limiter, LOCAL time step at CFL 0.9, FP64 plain path.
+One step = one SSP-RK3 iteration = 3 x num_cells cell-stage updates.  The mesh (~0.5 GB of
+device arrays) is larger than the 129 MB L2, so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--cells C]
+
+--impl reference times the reference's CPU solver step (the oracle port, a line-by-line
+restatement proven bit-identical to the reference) on the host cores: one independent replica of
+the same solve per core, a bounded number of iterations.
+Multi-GPU: replicas only (each rank advances its own copy of the solve; no collective on the path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+import __graft_entry__ as entry  # noqa: E402
+
+METRIC = "cell-stage updates/s"
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+
+def workload_case(pkg, cells):
+    mg = pkg.meshgen
+    u = mg.mach_speed(0.2)
+    mu = 1.225 * u * 1.0 / 100.0           # Re = rho u D / mu = 100
+    case = dict(mg.DEFAULT_CASE, eqn="NS", mu=mu, Pr=0.72, u=u, v=0.0, limiter="SQUEEZE", time_step_type="LOCAL",
+                CFL=0.9, BC1="NO_SLIP_WALL", BC2="FREESTREAM", solution_poly_order=1)
+    return case
+
+
+def make_grid(pkg, cells, seed=0):
+    return pkg.meshgen.voronoi_cylinder(cells, seed=seed)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def bytes_per_launch(kernel, N, F, ninc, Nb, s, ns, squeeze, stage_avg=True):
+    """Algorithmic bytes of one launch: every array element the kernel must touch, counted once.
+    s = state bytes (8 FP64, 4 FP32); integers 4 B; LSQ moments always 8 B."""
+    if kernel == "k_gradient":
+        b = N * (4 * s + 8 * s)                  # Q read, G write
+        if squeeze:
+            b += N * (4 * s + 8 * s)             # previous Q and limited G
+        b += N * 4 + ninc * 8 + N * 24           # CSR offsets, (face, neighbour) pairs, Ixx/Iyy/Ixy
+        b += F * s * (6 if squeeze else 2)       # dxj, dyj (+ c1dx, c1dy, c2dx, c2dy)
+        b += Nb * 2 * s                          # nx, ny on boundary faces
+        return b
+    if kernel == "k_face":
+        geo = 9 + (5 if ns else 0)
+        b = F * (8 + geo * s)                    # c1, c2, geometry
+        b += N * (4 * s + 8 * s)                 # Q and G of every cell
+        b += F * 4 * s                           # t written
+        b += (F * s) / 3.0 if stage_avg else 0   # spectral term, last stage only
+        return b
+    if kernel == "k_update":
+        b = N * 4 + ninc * 4 + F * 4 * s         # CSR, face contributions
+        b += N * s                               # volume
+        b += N * 4 * s * (1 + 2.0 / 3.0)         # Qn read; Q1/Q2 read on stages 2-3
+        b += N * 4 * s                           # new state written
+        b += N * s * (1 + 2.0 / 3.0) / 1.0       # dt written (stage 1) / read (stages 2-3)
+        b += (N * 4 * s) / 3.0                   # residual stored on the last stage
+        b += (F * s + N * s) / 3.0               # spectral sum (last stage)
+        return b
+    return 0.0
+
+
+def roofline(kt, N, F, ninc, Nb, s, ns, squeeze, peak):
+    per = {}
+    for k in ("k_gradient", "k_face", "k_update"):
+        ms, launches = kt.get(k, (0.0, 0))
+        if launches:
+            per[k] = dict(avg_ms=ms / launches, launches=launches, total_ms=ms,
+                          bytes=bytes_per_launch(k, N, F, ninc, Nb, s, ns, squeeze))
+    tot = sum(v["total_ms"] for v in per.values()) or 1.0
+    dom = max(per, key=lambda k: per[k]["total_ms"])
+    d = per[dom]
+    achieved = d["bytes"] / (d["avg_ms"] * 1e-3) / 1e9
+    return dom, {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                 "frac": round(achieved / peak, 4), "traffic": None, "kernel": dom,
+                 "kernel_avg_ms": round(d["avg_ms"], 4), "bytes_per_launch": int(d["bytes"]),
+                 "share": {k: round(v["total_ms"] / tot, 3) for k, v in per.items()}}, per
+
+
+def peaks():
+    try:
+        with open(PEAKS_FILE) as fh:
+            p = json.load(fh)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def cpu_baseline(pkg, orc, grid, case, iters):
+    o = orc.Oracle("port", grid=grid, case=case)
+    o.iterate(1)                                   # first iteration includes allocation warm-up
+    t = o.time_iterations(iters)
+    N = grid.num_cells
+    return 3.0 * N * iters / t, t
+
+
+def run_reference_arm(args):
+    """Oracle port on the host cores: one replica per core, same mesh and options."""
+    import multiprocessing as mp
+
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    pkg = entry.load_package()
+    orc = entry.load_oracle()
+    orc.build(ref_dir="/nonexistent")
+    grid = make_grid(pkg, args.cells)
+    case = workload_case(pkg, args.cells)
+    cores = args.cpu_cores or os.cpu_count() or 1
+    ctx = mp.get_context("fork")       # no CUDA in this process
+    q = ctx.Queue()
+
+    def worker(i):
+        o = orc.Oracle("port", grid=grid, case=case)
+        o.iterate(max(args.warmup, 1))
+        t = o.time_iterations(args.steps)
+        q.put(t)
+
+    t0 = time.time()
+    procs = [ctx.Process(target=worker, args=(i,)) for i in range(cores)]
+    for p in procs:
+        p.start()
+    ts = [q.get() for _ in procs]
+    for p in procs:
+        p.join()
+    wall = time.time() - t0
+    N = grid.num_cells
+    per_core = [3.0 * N * args.steps / t for t in ts]
+    value = sum(per_core)
+    line = {"metric": METRIC, "value": value, "unit": "cell-stage/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * max(ts) / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "ns_cylinder_voronoi", "cells": N, "faces": grid.num_faces, "precision": "fp64",
+                       "parallelism": f"{cores} independent CPU replicas"},
+            "cpu_baseline": {"value": value, "unit": "cell-stage/s", "cores": cores, "kind": "port",
+                             "sample": f"{args.steps} SSP-RK3 iterations of the {N}-cell solve per core, "
+                                       f"after {max(args.warmup, 1)} warm-up iterations",
+                             "single_core_value": statistics.median(per_core)},
+            "e2e": {"value": value, "unit": "cell-stage/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": round(wall, 1)}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu_arm(args):
+    import torch
+
+    ws, rank, local = dist_env()
+    pkg = entry.load_package()
+    pkg.build.build()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    torch.cuda.set_device(local)
+    t_mesh = time.time()
+    grid = make_grid(pkg, args.cells)
+    case = workload_case(pkg, args.cells)
+    t_mesh = time.time() - t_mesh
+    prec = pkg.FP64 if args.precision == "fp64" else pkg.FP32
+    N, F = grid.num_cells, grid.num_faces
+    Nb = int((grid.fc2 <= 0).sum())
+    ninc = 2 * F - Nb
+    s_bytes = 8 if prec == pkg.FP64 else 4
+
+    solver = pkg.Solver(grid, case, precision=prec)
+    stream = torch.cuda.ExternalStream(solver.stream())
+    solver.step(args.warmup)
+    solver.synchronize()
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    clocks = Clocks(local)
+    # ---- device-resident timed region (CUDA graph replay of whole iterations)
+    barrier()
+    torch.cuda.synchronize()
+    solver.synchronize()
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        solver.step(1)
+    e1.record(stream)
+    e1.synchronize()
+    solver.synchronize()
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    barrier()
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * 3.0 * N * args.steps / (ms * 1e-3)
+
+    # ---- per-kernel timing pass (events around every launch, eager launches)
+    solver.set_kernel_timing(True)
+    solver.step(args.steps)
+    kt = solver.kernel_times()
+    solver.set_kernel_timing(False)
+    peak, peak_kind = peaks()
+    dom, roof, per = roofline(kt, N, F, ninc, Nb, s_bytes, True, True, peak)
+    roof["peak_source"] = f"{peak_kind} hbm_gbs"
+    launches = sum(v[1] for k, v in kt.items() if k in ("k_gradient", "k_face", "k_update"))
+    gpu_launches = 3 * 3 * args.steps
+
+    # ---- end to end through the C ABI with host buffers: upload Qbar, one iteration, download
+    q = solver.get_state()
+    norm = np.zeros(4)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        solver.load_state(q)
+        solver.step(1)
+        solver.get_state(q)
+        norm = solver.residual_norm()
+    t_e2e = time.perf_counter() - t0
+    e2e = {"value": ws * 3.0 * N * args.steps / t_e2e, "unit": "cell-stage/s",
+           "h2d_bytes_per_step": 4 * 8 * N, "d2h_bytes_per_step": 4 * 8 * N + 4 * 8}
+
+    # ---- CPU baseline (oracle port, 1 core, bounded sample)
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        orc = entry.load_oracle()
+        orc.build(ref_dir="/nonexistent")
+        cv, ct = cpu_baseline(pkg, orc, grid, case, args.cpu_iters)
+        cpu = {"value": cv, "unit": "cell-stage/s", "cores": 1, "kind": "port",
+               "sample": f"{args.cpu_iters} SSP-RK3 iterations of the same {N}-cell solve ({ct:.1f} s), after 1 warm-up"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "cell-stage/s", "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64" if prec == pkg.FP64 else "f32", "data": "synthetic",
+                "config": {"workload": "ns_cylinder_voronoi", "cells": N, "faces": F, "boundary_faces": Nb,
+                           "max_sides": max(grid.sides_histogram()), "precision": args.precision,
+                           "re": 100, "mach": 0.2, "limiter": "SQUEEZE", "dt": "LOCAL", "cfl": 0.9,
+                           "l2": "working set > L2 (no flush)", "parallelism": f"{ws} replicas" if ws > 1 else "single GPU",
+                           "mesh_gen_s": round(t_mesh, 1)},
+                "clocks": clk, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": gpu_launches,
+                "kernels": {k: {"avg_ms": round(v["avg_ms"], 4), "launches": v["launches"],
+                                "bytes_per_launch": int(v["bytes"]),
+                                "gbs": round(v["bytes"] / (v["avg_ms"] * 1e-3) / 1e9, 1)} for k, v in per.items()},
+                "residual_norm": [float(x) for x in norm], "device_bytes": solver.device_bytes()}
+        print(json.dumps(line), flush=True)
+    solver.close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cells", type=int, default=1_000_000)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--cpu-iters", type=int, default=4)
+    ap.add_argument("--cpu-cores", type=int, default=0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference_arm(args)
+    else:
+        run_gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,246 @@
+// C ABI of the GB300 fv2d library (declared in include/fv2d_gpu.h).
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "fv2d_gpu.h"
+#include "fv2d_host.h"
+#include "fv2d_solver.h"
+
+namespace fv2d {
+const char* const kKernelNames[K_COUNT] = {"k_gradient", "k_face", "k_update", "k_spectral_init",
+                                          "k_state_in", "k_state_out", "k_res_norm_partial"};
+}
+
+struct fv2d_handle {
+    std::unique_ptr<fv2d::Solver> s;
+    int precision = FV2D_FP64;
+};
+
+struct fv2d_mesh {
+    fv2d::HostMesh m;
+};
+
+namespace {
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+// Options the reference's solver step implements (res.cpp:26-69, ssp_rk3.cpp, main.cpp:122-127).
+int check_case(const fv2d_case* cs) {
+    if (!cs) return fail(FV2D_ERR_ARG, "null case");
+    if (cs->order != 1 && cs->order != 2)
+        return fail(FV2D_ERR_CASE, "solution_poly_order must be 0 or 1 (res.cpp:56-58 rejects other orders)");
+    if (cs->eqn != FV2D_EULER && cs->eqn != FV2D_NS) return fail(FV2D_ERR_CASE, "eqn must be EULER or NS");
+    if (cs->flux_solver != FV2D_RUSANOV)
+        return fail(FV2D_ERR_CASE, "flux_solver must be RUSANOV (the reference's ROE path is unfinished: res.cpp:66-68)");
+    if (cs->limiter != FV2D_LIM_NONE && cs->limiter != FV2D_LIM_MINMOD && cs->limiter != FV2D_LIM_SQUEEZE)
+        return fail(FV2D_ERR_CASE, "limiter must be NONE, MINMOD or SQUEEZE");
+    if (cs->time_type != FV2D_DT_GLOBAL && cs->time_type != FV2D_DT_LOCAL)
+        return fail(FV2D_ERR_CASE, "time_step_type must be GLOBAL or LOCAL");
+    for (int b : {cs->bc1, cs->bc2})
+        if (b > -1 || b < -4) return fail(FV2D_ERR_CASE, "BC1/BC2 must be FREESTREAM, SLIP_WALL, EXTRAPOLATION or NO_SLIP_WALL");
+    if (!(cs->gamma > 1) || !(cs->R > 0) || !(cs->rho > 0) || !(cs->P > 0))
+        return fail(FV2D_ERR_CASE, "gamma > 1, R > 0, rho > 0 and P > 0 are required");
+    if (cs->eqn == FV2D_NS && !(cs->Pr > 0)) return fail(FV2D_ERR_CASE, "NS needs Pr > 0");
+    if (!(cs->cfl > 0)) return fail(FV2D_ERR_CASE, "CFL must be > 0");
+    return FV2D_OK;
+}
+
+int check_device() {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) return fail(FV2D_ERR_NODEV, std::string("no CUDA device: ") + cudaGetErrorString(e));
+    return FV2D_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int fv2d_read_inputs(const char* path, fv2d_case* out) {
+    if (!path || !out) return fail(FV2D_ERR_ARG, "null argument");
+    std::string err;
+    int rc = fv2d::parse_inputs(path, out, err);
+    if (rc) g_err = err;
+    return rc;
+}
+
+int fv2d_read_grid(const char* path, int* num_points, int* num_faces, int* num_cells, double** x, double** y,
+                   int** face_point1, int** face_point2, int** face_cell1, int** face_cell2) {
+    if (!path || !num_points || !num_faces || !num_cells || !x || !y || !face_point1 || !face_point2 || !face_cell1 || !face_cell2)
+        return fail(FV2D_ERR_ARG, "null argument");
+    std::vector<double> vx, vy;
+    std::vector<int> a, b, c, d;
+    int nc = 0;
+    std::string err;
+    int rc = fv2d::parse_grid(path, vx, vy, a, b, c, d, nc, err);
+    if (rc) return fail(rc, err);
+    auto dup = [](const void* src, size_t bytes) { void* p = std::malloc(bytes ? bytes : 1); std::memcpy(p, src, bytes); return p; };
+    *num_points = (int)vx.size(); *num_faces = (int)a.size(); *num_cells = nc;
+    *x = (double*)dup(vx.data(), 8 * vx.size());
+    *y = (double*)dup(vy.data(), 8 * vy.size());
+    *face_point1 = (int*)dup(a.data(), 4 * a.size());
+    *face_point2 = (int*)dup(b.data(), 4 * b.size());
+    *face_cell1 = (int*)dup(c.data(), 4 * c.size());
+    *face_cell2 = (int*)dup(d.data(), 4 * d.size());
+    return FV2D_OK;
+}
+
+void fv2d_free(void* p) { std::free(p); }
+
+int fv2d_mesh_build(const fv2d_mesh_desc* desc, const fv2d_case* cs, fv2d_mesh** out) {
+    if (!out) return fail(FV2D_ERR_ARG, "null output");
+    *out = nullptr;
+    int rc = check_case(cs);
+    if (rc) return rc;
+    auto m = std::make_unique<fv2d_mesh>();
+    std::string err;
+    rc = fv2d::build_mesh(desc, cs, m->m, err);
+    if (rc) return fail(rc, err);
+    *out = m.release();
+    return FV2D_OK;
+}
+
+void fv2d_mesh_free(fv2d_mesh* m) { delete m; }
+
+int fv2d_mesh_sizes(const fv2d_mesh* mm, int* o) {
+    if (!mm || !o) return fail(FV2D_ERR_ARG, "null argument");
+    const fv2d::HostMesh& m = mm->m;
+    o[0] = m.np; o[1] = m.nf; o[2] = m.nc; o[3] = m.numBC1; o[4] = m.numBC2; o[5] = m.numWALL;
+    o[6] = m.num_of_BC; o[7] = m.max_sides;
+    return FV2D_OK;
+}
+
+int fv2d_mesh_get(const fv2d_mesh* mm, int field, double* out) {
+    if (!mm || !out) return fail(FV2D_ERR_ARG, "null argument");
+    return fv2d::mesh_field(mm->m, field, out) < 0 ? fail(FV2D_ERR_ARG, "unknown mesh field") : FV2D_OK;
+}
+
+int fv2d_mesh_permutation(const fv2d_mesh* mm, int kind, int* out) {
+    if (!mm || !out) return fail(FV2D_ERR_ARG, "null argument");
+    const std::vector<int>& p = kind == 0 ? mm->m.cell_new2old : mm->m.face_new2old;
+    std::copy(p.begin(), p.end(), out);
+    return FV2D_OK;
+}
+
+int fv2d_create(const fv2d_mesh_desc* desc, const fv2d_case* cs, int precision, fv2d_handle** out) {
+    if (!out) return fail(FV2D_ERR_ARG, "null output");
+    *out = nullptr;
+    int rc = check_case(cs);
+    if (rc) return rc;
+    if (precision != FV2D_FP64 && precision != FV2D_FP32) return fail(FV2D_ERR_ARG, "precision must be FV2D_FP64 or FV2D_FP32");
+    if ((rc = check_device())) return rc;
+    auto h = std::make_unique<fv2d_handle>();
+    h->precision = precision;
+    h->s.reset(precision == FV2D_FP64 ? fv2d::make_solver_fp64() : fv2d::make_solver_fp32());
+    std::string err;
+    rc = fv2d::build_mesh(desc, cs, h->s->mesh_, err);
+    if (rc) return fail(rc, err);
+    rc = h->s->init(*cs);
+    if (rc) return fail(rc, h->s->err_);
+    *out = h.release();
+    return FV2D_OK;
+}
+
+int fv2d_create_from_files(const char* input_path, int precision, fv2d_handle** out) {
+    if (!input_path || !out) return fail(FV2D_ERR_ARG, "null argument");
+    *out = nullptr;
+    fv2d_case cs;
+    int rc = fv2d_read_inputs(input_path, &cs);
+    if (rc) return rc;
+    std::vector<double> x, y;
+    std::vector<int> a, b, c, d;
+    int nc = 0;
+    std::string err;
+    rc = fv2d::parse_grid(cs.grid_file, x, y, a, b, c, d, nc, err);   // relative to the working directory, like readmesh
+    if (rc) return fail(rc, err);
+    fv2d_mesh_desc desc{(int)x.size(), (int)a.size(), nc, x.data(), y.data(), a.data(), b.data(), c.data(), d.data()};
+    return fv2d_create(&desc, &cs, precision, out);
+}
+
+void fv2d_destroy(fv2d_handle* h) { delete h; }
+
+#define FV2D_H(h) if (!(h) || !(h)->s) return fail(FV2D_ERR_ARG, "null handle")
+#define FV2D_RET(h, expr) do { int rc_ = (expr); if (rc_) g_err = (h)->s->err_; return rc_; } while (0)
+
+int fv2d_step(fv2d_handle* h, int iterations) { FV2D_H(h); FV2D_RET(h, h->s->step(iterations)); }
+int fv2d_stage(fv2d_handle* h) { FV2D_H(h); FV2D_RET(h, h->s->stage()); }
+
+int fv2d_set_state(fv2d_handle* h, const double* q) {
+    FV2D_H(h);
+    if (!q) return fail(FV2D_ERR_ARG, "null state");
+    FV2D_RET(h, h->s->set_state(q));
+}
+
+int fv2d_load_state(fv2d_handle* h, const double* q) {
+    FV2D_H(h);
+    if (!q) return fail(FV2D_ERR_ARG, "null state");
+    FV2D_RET(h, h->s->load_state(q));
+}
+
+int fv2d_get_state(fv2d_handle* h, double* q) {
+    FV2D_H(h);
+    if (!q) return fail(FV2D_ERR_ARG, "null output");
+    FV2D_RET(h, h->s->get_field(FV2D_F_QBAR, q));
+}
+
+int fv2d_get_field(fv2d_handle* h, int field, double* out) {
+    FV2D_H(h);
+    if (!out) return fail(FV2D_ERR_ARG, "null output");
+    FV2D_RET(h, h->s->get_field(field, out));
+}
+
+int fv2d_residual_norm(fv2d_handle* h, double out4[4]) {
+    FV2D_H(h);
+    if (!out4) return fail(FV2D_ERR_ARG, "null output");
+    FV2D_RET(h, h->s->residual_norm(out4));
+}
+
+int fv2d_sizes(fv2d_handle* h, int* o) {
+    FV2D_H(h);
+    if (!o) return fail(FV2D_ERR_ARG, "null output");
+    const fv2d::HostMesh& m = h->s->mesh_;
+    o[0] = m.np; o[1] = m.nf; o[2] = m.nc; o[3] = m.numBC1; o[4] = m.numBC2; o[5] = m.numWALL;
+    o[6] = m.num_of_BC; o[7] = h->s->current_stage();
+    return FV2D_OK;
+}
+
+int fv2d_synchronize(fv2d_handle* h) { FV2D_H(h); FV2D_RET(h, h->s->synchronize()); }
+int fv2d_set_store_residual(fv2d_handle* h, int every) { FV2D_H(h); FV2D_RET(h, h->s->set_store_residual(every)); }
+int fv2d_set_graphs(fv2d_handle* h, int enable) { FV2D_H(h); FV2D_RET(h, h->s->set_graphs(enable)); }
+int fv2d_set_kernel_timing(fv2d_handle* h, int enable) { FV2D_H(h); FV2D_RET(h, h->s->set_timing(enable)); }
+
+int fv2d_kernel_times(fv2d_handle* h, char* names, int names_len, double* ms, int* launches, int max_kernels, int* n_kernels) {
+    FV2D_H(h);
+    double t[fv2d::K_COUNT];
+    int l[fv2d::K_COUNT];
+    int rc = h->s->kernel_times(t, l);
+    if (rc) return fail(rc, h->s->err_);
+    const int n = max_kernels < fv2d::K_COUNT ? max_kernels : fv2d::K_COUNT;
+    std::string all;
+    for (int i = 0; i < n; i++) {
+        if (ms) ms[i] = t[i];
+        if (launches) launches[i] = l[i];
+        if (i) all += ",";
+        all += fv2d::kKernelNames[i];
+    }
+    if (names && names_len > 0) std::snprintf(names, names_len, "%s", all.c_str());
+    if (n_kernels) *n_kernels = n;
+    return FV2D_OK;
+}
+
+void* fv2d_stream(fv2d_handle* h) { return (h && h->s) ? h->s->stream() : nullptr; }
+long long fv2d_device_bytes(fv2d_handle* h) { return (h && h->s) ? h->s->device_bytes() : 0; }
+
+const char* fv2d_last_error(fv2d_handle* h) {
+    if (h && h->s && !h->s->err_.empty()) return h->s->err_.c_str();
+    return g_err.c_str();
+}
+
+}  // extern "C"

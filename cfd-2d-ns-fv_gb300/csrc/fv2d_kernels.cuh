@@ -1,0 +1,471 @@
+// Device kernels of the fv2d residual-and-update step, templated on the state precision T.
+//
+// One RK stage = three launches:
+//   k_gradient  (one thread per cell)  LSQ gradient over the cell's faces + squeeze limiter
+//   k_face      (one thread per face)  reconstruction, boundary ghosts, NS face terms, Rusanov
+//                                      flux; writes the face's residual contribution
+//   k_update    (one thread per cell)  gathers the face contributions in ascending original face
+//                                      id, divides by the volume, applies the SSP-RK3 stage, and
+//                                      (last stage) the spectral sums for the next time step
+// Every per-cell sum visits the cell's faces in ascending ORIGINAL face id, the order in which
+// the reference's face loops scatter into the cell, so with T = double and FMA contraction off
+// (-fmad=false) the results are bit-identical to the reference; no atomics touch the state.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace fv2d {
+
+template <class T>
+struct alignas(4 * sizeof(T)) Q4 {
+    T p[4];
+};
+
+template <class T>
+struct Consts {
+    T gamma, gm1, R, mu, k;            // gm1 = gamma - 1, k = mu*Cp/Pr (class_flow.hpp:36-40)
+    T q_inf[4];                        // freestream conservative state (class_flow.hpp:28-34)
+    T rho_inf, u_inf, v_inf, P_inf;    // freestream primitives (initial Qbar primitives)
+    T two_cfl;                         // 2*CFL
+    T vn0, c0;                         // initial Vn_avg, c_avg (class_q.hpp:61-62)
+};
+
+// Face geometry, SoA, device order.
+template <class T>
+struct FaceGeo {
+    const T *nx, *ny, *area, *c1dx, *c1dy, *c2dx, *c2dy, *dxj, *dyj, *mx, *my, *lx, *ly, *dist;
+};
+
+template <class T>
+__device__ __forceinline__ Q4<T> ldq(const Q4<T>* __restrict__ a, int i) {
+    return a[i];
+}
+
+// std::min({a, b}) / std::max({a, b}) semantics (first argument wins ties)
+template <class T>
+__device__ __forceinline__ T min2(T a, T b) { return (b < a) ? b : a; }
+template <class T>
+__device__ __forceinline__ T max2(T a, T b) { return (a < b) ? b : a; }
+
+// class_Q::updateflow for one state (class_q.hpp:131-141); T (temperature) is never read by the
+// step and is not formed.
+template <class T>
+__device__ __forceinline__ void prims(const T p[4], const Consts<T>& k, T& rho, T& u, T& v, T& P) {
+    rho = p[0];
+    const T E = p[3];
+    u = p[1] / rho;
+    v = p[2] / rho;
+    P = (E - (T(0.5) * rho * (u * u + v * v))) * k.gm1;
+}
+
+// class_flow::updateQ (class_flow.hpp:28-34)
+template <class T>
+__device__ __forceinline__ void cons(T rho, T u, T v, T P, const Consts<T>& k, T q[4]) {
+    q[0] = rho;
+    q[1] = rho * u;
+    q[2] = rho * v;
+    q[3] = (P / k.gm1) + T(0.5) * rho * (u * u + v * v);
+}
+
+// ------------------------------------------------------------------------------------------
+// Gradient + squeeze limiter.  compute_gradient (src/solver/cell_gradient.cpp:9-131) and
+// squeeze (src/solver/squeeze.cpp:9-155), restated as one gather per cell.
+// The squeeze compares against the face values of the PREVIOUS stage (res.cpp:40 runs before the
+// reconstruction at :48); they are recomputed here from the previous stage's state and limited
+// gradient with the reconstruction's own expression, or are the -101 sentinel the face states
+// start with (class_q.hpp:73-76) on the first stage after initialisation.
+template <class T, bool SQUEEZE>
+__global__ void __launch_bounds__(256)
+k_gradient(int nc, const int* __restrict__ inc_off, const int* __restrict__ inc, const int* __restrict__ nbr,
+           const int* __restrict__ qcell, FaceGeo<T> g, const double* __restrict__ Ixx,
+           const double* __restrict__ Iyy, const double* __restrict__ Ixy, const Q4<T>* __restrict__ Q,
+           const Q4<T>* __restrict__ Qprev, const Q4<T>* __restrict__ Gprev, Q4<T>* __restrict__ Gout,
+           Consts<T> k, int first_stage, int init_prims) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    const Q4<T> qc = ldq(Q, c);
+    T sx[4] = {T(0), T(0), T(0), T(0)}, sy[4] = {T(0), T(0), T(0), T(0)};
+    T qmin[4], qmax[4];
+    if (SQUEEZE)
+        for (int j = 0; j < 4; j++) { qmin[j] = T(100000000000.0); qmax[j] = T(-100000000000.0); }
+    const int b = inc_off[c], e = inc_off[c + 1];
+    for (int i = b; i < e; i++) {
+        const int f = inc[i] >> 1, side = inc[i] & 1, nb = nbr[i];
+        T d[4];
+        if (nb >= 0) {
+            const Q4<T> qn = ldq(Q, nb);
+            const T* q1 = side == 0 ? qc.p : qn.p;   // reference orientation: c2 - c1
+            const T* q2 = side == 0 ? qn.p : qc.p;
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                d[j] = q2[j] - q1[j];
+                if (SQUEEZE) {
+                    qmin[j] = min2(qmin[j], min2(q1[j], q2[j]));
+                    qmax[j] = max2(qmax[j], max2(q1[j], q2[j]));
+                }
+            }
+        } else {
+            if (nb == -1) {
+#pragma unroll
+                for (int j = 0; j < 4; j++) d[j] = k.q_inf[j] - qc.p[j];
+            } else if (nb == -2 || nb == -4) {
+                T rho, u, v, P;
+                if (init_prims) { rho = k.rho_inf; u = k.u_inf; v = k.v_inf; P = k.P_inf; }
+                else if (nb == -2) prims(qc.p, k, rho, u, v, P);
+                else { const Q4<T> qq = ldq(Q, qcell[f]); prims(qq.p, k, rho, u, v, P); }
+                T gq[4];
+                if (nb == -2) {        // slip wall: reflect the cell velocity (cell_gradient.cpp:43-55)
+                    const T fnx = g.nx[f], fny = g.ny[f];
+                    const T vn = u * fnx + v * fny;
+                    cons(rho, u - T(2.0) * vn * fnx, v - T(2.0) * vn * fny, P, k, gq);
+                } else {               // no-slip: state of cell `face id`, velocity negated (:62-73)
+                    cons(rho, -u, -v, P, k, gq);
+                }
+#pragma unroll
+                for (int j = 0; j < 4; j++) d[j] = gq[j] - qc.p[j];
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; j++) d[j] = T(0);
+            }
+            if (SQUEEZE)
+#pragma unroll
+                for (int j = 0; j < 4; j++) { qmin[j] = min2(qmin[j], qc.p[j]); qmax[j] = max2(qmax[j], qc.p[j]); }
+        }
+        const T fx = g.dxj[f], fy = g.dyj[f];
+#pragma unroll
+        for (int j = 0; j < 4; j++) { sx[j] += d[j] * fx; sy[j] += d[j] * fy; }
+    }
+    const T ixx = (T)Ixx[c], iyy = (T)Iyy[c], ixy = (T)Ixy[c];
+    Q4<T> gx, gy;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        gx.p[j] = (sx[j] * iyy - sy[j] * ixy);
+        gy.p[j] = (sy[j] * ixx - sx[j] * ixy);
+    }
+    if (SQUEEZE) {
+        T phi[4] = {T(1), T(1), T(1), T(1)};
+        Q4<T> qp, gpx, gpy;
+        if (!first_stage) { qp = ldq(Qprev, c); gpx = ldq(Gprev, 2 * c); gpy = ldq(Gprev, 2 * c + 1); }
+        for (int i = b; i < e; i++) {
+            const int f = inc[i] >> 1, side = inc[i] & 1;
+            const T dx = side == 0 ? g.c1dx[f] : g.c2dx[f];
+            const T dy = side == 0 ? g.c1dy[f] : g.c2dy[f];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const T qf = first_stage ? T(-101) : qp.p[j] + gpx.p[j] * dx + gpy.p[j] * dy;
+                T ph = T(1);
+                if (qf < qmin[j]) ph = (qmin[j] - qc.p[j]) / (qf - qc.p[j]);
+                else if (qf > qmax[j]) ph = (qmax[j] - qc.p[j]) / (qf - qc.p[j]);
+                phi[j] = min2(ph, phi[j]);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j++) { gx.p[j] = gx.p[j] * phi[j]; gy.p[j] = gy.p[j] * phi[j]; }
+    }
+    Gout[2 * c] = gx;
+    Gout[2 * c + 1] = gy;
+}
+
+// ------------------------------------------------------------------------------------------
+// Face kernel: reconstruction + boundary ghosts (reconstruction.cpp:22-80), NS face terms
+// (reconstruction.cpp:86-164, class_q.hpp:163-169, class_f.hpp:52-59), Rusanov flux
+// (class_f.hpp:41-50, rusanov.cpp:20-36) and the face's residual contribution (res.cpp:81-89).
+// Writes t = (V*A) - (F*A) per face and, on the last stage of an iteration, the spectral term
+// (|Vn_avg| + c_avg)*A that the next time step sums (ssp_rk3.cpp:28-36).
+template <class T, bool ORDER2, bool NS, bool LAST>
+__global__ void __launch_bounds__(256)
+k_face(int nf, const int* __restrict__ fc1, const int* __restrict__ fc2, FaceGeo<T> g,
+       const Q4<T>* __restrict__ Q, const Q4<T>* __restrict__ G, Q4<T>* __restrict__ tout,
+       T* __restrict__ sout, Consts<T> k, int init_prims) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nf) return;
+    const int c1 = fc1[f], c2 = fc2[f];
+    const T fnx = g.nx[f], fny = g.ny[f], A = g.area[f];
+    const Q4<T> q1 = ldq(Q, c1);
+    Q4<T> g1x, g1y;
+    if (ORDER2) { g1x = ldq(G, 2 * c1); g1y = ldq(G, 2 * c1 + 1); }
+    else {
+#pragma unroll
+        for (int j = 0; j < 4; j++) { g1x.p[j] = T(0); g1y.p[j] = T(0); }
+    }
+    T L[4], Rq[4];
+    {
+        const T dx = g.c1dx[f], dy = g.c1dy[f];
+#pragma unroll
+        for (int j = 0; j < 4; j++) L[j] = q1.p[j] + g1x.p[j] * dx + g1y.p[j] * dy;
+    }
+    T lrho, lu, lv, lP;
+    prims(L, k, lrho, lu, lv, lP);
+    const T lc = sqrt(k.gamma * (lP / lrho));
+    Q4<T> q2, g2x, g2y;
+    if (c2 >= 0) {
+        q2 = ldq(Q, c2);
+        if (ORDER2) { g2x = ldq(G, 2 * c2); g2y = ldq(G, 2 * c2 + 1); }
+        else {
+#pragma unroll
+            for (int j = 0; j < 4; j++) { g2x.p[j] = T(0); g2y.p[j] = T(0); }
+        }
+        const T dx = g.c2dx[f], dy = g.c2dy[f];
+#pragma unroll
+        for (int j = 0; j < 4; j++) Rq[j] = q2.p[j] + g2x.p[j] * dx + g2y.p[j] * dy;
+    } else if (c2 == -1) {
+#pragma unroll
+        for (int j = 0; j < 4; j++) Rq[j] = k.q_inf[j];
+    } else if (c2 == -2) {
+        const T vn = lu * fnx + lv * fny;
+        cons(lrho, lu - T(2.0) * vn * fnx, lv - T(2.0) * vn * fny, lP, k, Rq);
+    } else if (c2 == -3) {
+#pragma unroll
+        for (int j = 0; j < 4; j++) Rq[j] = L[j];
+    } else {
+        cons(lrho, -lu, -lv, lP, k, Rq);
+    }
+    T rrho, ru, rv, rP;
+    prims(Rq, k, rrho, ru, rv, rP);
+    const T rc = sqrt(k.gamma * (rP / rrho));
+
+    // Rusanov
+    const T vn1 = lu * fnx + lv * fny;
+    const T vn2 = ru * fnx + rv * fny;
+    const T F1[4] = {lrho * vn1, lrho * lu * vn1 + lP * fnx, lrho * lv * vn1 + lP * fny, vn1 * (L[3] + lP)};
+    const T F2[4] = {rrho * vn2, rrho * ru * vn2 + rP * fnx, rrho * rv * vn2 + rP * fny, vn2 * (Rq[3] + rP)};
+    const T vna = (vn1 + vn2) / T(2);
+    const T ca = (lc + rc) / T(2);
+    const T lam = (fabs(vna) + ca) / T(2);
+    T Fr[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) Fr[j] = (F1[j] + F2[j]) / T(2) - lam * (Rq[j] - L[j]);
+
+    // viscous flux (first order never adds it: res.cpp:27-29,50-53)
+    T V[4] = {T(0), T(0), T(0), T(0)};
+    if (NS && ORDER2) {
+        T Aq[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) Aq[j] = T(0.5) * (L[j] + Rq[j]);
+        T arho, au, av, aP;
+        prims(Aq, k, arho, au, av, aP);
+        T ux = T(0), uy = T(0), vx = T(0), vy = T(0), Px = T(0), Py = T(0), rx = T(0), ry = T(0);
+        bool have = true;
+        if (c2 >= 0) {
+            const T ad = fabs(g.dist[f]);
+            const T mxf = g.mx[f], myf = g.my[f], lxf = g.lx[f], lyf = g.ly[f];
+            T dQx[4], dQy[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const T dl = (q2.p[j] - q1.p[j]) / ad;
+                const T dm = T(0.5) * (g1x.p[j] * mxf + g1y.p[j] * myf + g2x.p[j] * mxf + g2y.p[j] * myf);
+                dQy[j] = dl * lyf + dm * lyf;
+                dQx[j] = dl * lxf + dm * lxf;
+            }
+            rx = dQx[0];
+            ux = dQx[1] - rx * au / arho;
+            vx = dQx[2] - rx * av / arho;
+            ry = dQy[0];
+            uy = dQy[1] - ry * au / arho;
+            vy = dQy[2] - ry * au / arho;          // reconstruction.cpp:155 uses u
+            Px = k.gm1 * (dQx[3] - T(0.5) * rx * (au * au + av * av) - arho * (au * ux + av * vx));
+            Py = k.gm1 * (dQy[3] - T(0.5) * ry * (au * au + av * av) - arho * (au * uy + av * vy));
+        } else if (c2 == -4) {
+            const T d1x = g.c1dx[f], d1y = g.c1dy[f];
+            const T dn = fabs(sqrt(d1x * d1x + d1y * d1y));
+            T cu, cv;
+            if (init_prims) { cu = k.u_inf; cv = k.v_inf; }
+            else { cu = q1.p[1] / q1.p[0]; cv = q1.p[2] / q1.p[0]; }
+            const T dudn = -cu / dn, dvdn = -cv / dn;
+            ux = dudn * fnx; uy = dudn * fny;
+            vx = dvdn * fnx; vy = dvdn * fny;
+        } else if (c2 == -2) {
+            have = false;   // SLIP_WALL with NS: tau and grad T keep their initial zeros (:104-106)
+        }
+        T txx, txy, tyy, dTx, dTy;
+        if (have) {
+            txx = T(2) * k.mu * (ux - (ux + vy) / T(3));
+            txy = k.mu * (uy + vx);
+            tyy = T(2) * k.mu * (vy - (ux + vy) / T(3));
+            dTx = (Px * arho - rx * aP) / (k.R * arho * arho);
+            dTy = (Py * arho - ry * aP) / (k.R * arho * arho);
+        } else {
+            txx = T(0); txy = T(0); tyy = T(0); dTx = T(0); dTy = T(0);
+        }
+        V[0] = T(0);
+        V[1] = txx * fnx + txy * fny;
+        V[2] = txy * fnx + tyy * fny;
+        V[3] = fnx * (au * txx + av * txy + k.k * dTx) + fny * (au * txy + av * tyy + k.k * dTy);
+    }
+    Q4<T> t;
+#pragma unroll
+    for (int j = 0; j < 4; j++) t.p[j] = (V[j] * A) - (Fr[j] * A);
+    tout[f] = t;
+    if (LAST) sout[f] = (fabs(vna) + ca) * A;
+}
+
+// ------------------------------------------------------------------------------------------
+// Spectral sums S_c = sum_f (|Vn_avg| + c_avg) A_f in ascending original face id
+// (ssp_rk3.cpp:28-36).  s == nullptr: the initial Vn_avg, c_avg of every face (class_q.hpp:61-62).
+template <class T>
+__device__ __forceinline__ void atomic_max_pos(T* addr, T v);
+template <>
+__device__ __forceinline__ void atomic_max_pos<double>(double* addr, double v) {
+    atomicMax(reinterpret_cast<unsigned long long*>(addr), (unsigned long long)__double_as_longlong(v));
+}
+template <>
+__device__ __forceinline__ void atomic_max_pos<float>(float* addr, float v) {
+    atomicMax(reinterpret_cast<unsigned int*>(addr), __float_as_uint(v));
+}
+
+template <class T>
+__device__ __forceinline__ T block_max(T v) {
+    __shared__ T red[32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max2(v, __shfl_xor_sync(0xffffffffu, v, o));
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) red[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        v = lane < (int)(blockDim.x >> 5) ? red[lane] : T(0);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = max2(v, __shfl_xor_sync(0xffffffffu, v, o));
+    }
+    return v;
+}
+
+template <class T>
+__global__ void __launch_bounds__(256)
+k_spectral_init(int nc, const int* __restrict__ inc_off, const int* __restrict__ inc, const T* __restrict__ area,
+                T* __restrict__ S, T* __restrict__ smax, Consts<T> k) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    T s = T(0);
+    if (c < nc) {
+        for (int i = inc_off[c]; i < inc_off[c + 1]; i++) s += (fabs(k.vn0) + k.c0) * area[inc[i] >> 1];
+        S[c] = s;
+    }
+    const T m = block_max(c < nc ? s : T(0));
+    if (threadIdx.x == 0) atomic_max_pos(smax, m);
+}
+
+// ------------------------------------------------------------------------------------------
+// Residual gather + SSP-RK3 stage (res.cpp:74-109, ssp_rk3.cpp:38-77).
+// STAGE 0: dt from the spectral sums (GLOBAL: 2*CFL*vol/max S, LOCAL: 2*CFL*vol/S), Q1 = Qn+dt*R
+// STAGE 1: Q2 = 0.75*Qn + 0.25*Q1 + 0.25*dt*R
+// STAGE 2: Qn = 1/3*Qn + 2/3*Q2 + 2/3*dt*R, and the spectral sums for the next iteration.
+// Non-physical results (rho <= 0, E <= 0, NaN) raise bit 0 of *flag; values are kept as computed.
+template <class T, int STAGE>
+__global__ void __launch_bounds__(256)
+k_update(int nc, const int* __restrict__ inc_off, const int* __restrict__ inc, const Q4<T>* __restrict__ tface,
+         const T* __restrict__ sface, const T* __restrict__ vol, Q4<T>* __restrict__ Qn, Q4<T>* __restrict__ Q1,
+         Q4<T>* __restrict__ Q2, T* __restrict__ dt, T* __restrict__ S, T* __restrict__ smax, Q4<T>* __restrict__ Rout,
+         int* __restrict__ flag, Consts<T> k, int global_dt) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    T snext = T(0);
+    if (c < nc) {
+        T r[4] = {T(0), T(0), T(0), T(0)};
+        const int b = inc_off[c], e = inc_off[c + 1];
+        for (int i = b; i < e; i++) {
+            const int f = inc[i] >> 1;
+            const Q4<T> t = ldq(tface, f);
+            if (inc[i] & 1) {
+#pragma unroll
+                for (int j = 0; j < 4; j++) r[j] -= t.p[j];
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; j++) r[j] += t.p[j];
+            }
+        }
+        const T vc = vol[c];
+#pragma unroll
+        for (int j = 0; j < 4; j++) r[j] = r[j] / vc;
+        if (Rout) { Q4<T> rr; for (int j = 0; j < 4; j++) rr.p[j] = r[j]; Rout[c] = rr; }
+        const Q4<T> qn = ldq(Qn, c);
+        Q4<T> out;
+        T dtc;
+        if (STAGE == 0) {
+            dtc = (k.two_cfl * vc) / (global_dt ? *smax : S[c]);
+            dt[c] = dtc;
+#pragma unroll
+            for (int j = 0; j < 4; j++) out.p[j] = qn.p[j] + dtc * r[j];
+            Q1[c] = out;
+        } else if (STAGE == 1) {
+            dtc = dt[c];
+            const Q4<T> q1 = ldq(Q1, c);
+#pragma unroll
+            for (int j = 0; j < 4; j++) out.p[j] = T(0.75) * qn.p[j] + T(0.25) * q1.p[j] + T(0.25) * dtc * r[j];
+            Q2[c] = out;
+        } else {
+            dtc = dt[c];
+            const Q4<T> q2 = ldq(Q2, c);
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+                out.p[j] = T(1.0 / 3.0) * qn.p[j] + T(2.0 / 3.0) * q2.p[j] + T(2.0 / 3.0) * dtc * r[j];
+            Qn[c] = out;
+            for (int i = b; i < e; i++) snext += sface[inc[i] >> 1];
+            S[c] = snext;
+        }
+        if (!(out.p[0] > T(0)) || !(out.p[3] > T(0))) atomicOr(flag, 1);
+    }
+    if (STAGE == 2) {
+        const T m = block_max(c < nc ? snext : T(0));
+        if (threadIdx.x == 0) atomic_max_pos(smax, m);
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Host-format <-> device-format state (SoA double in file numbering <-> AoS T in device order).
+template <class T>
+__global__ void k_state_in(int nc, const int* __restrict__ new2old, const double* __restrict__ q, Q4<T>* __restrict__ Q) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    const int o = new2old[c];
+    Q4<T> v;
+#pragma unroll
+    for (int j = 0; j < 4; j++) v.p[j] = (T)q[(size_t)j * nc + o];
+    Q[c] = v;
+}
+
+template <class T>
+__global__ void k_state_out(int nc, int ncomp, const int* __restrict__ new2old, const Q4<T>* __restrict__ Q,
+                            double* __restrict__ q) {
+    // ncomp = 4 (state) or 8 (gradient pairs: x block then y block)
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    const int o = new2old[c];
+    const int per = ncomp / 4;
+    for (int h = 0; h < per; h++) {
+        const Q4<T> v = Q[(size_t)per * c + h];
+#pragma unroll
+        for (int j = 0; j < 4; j++) q[(size_t)(4 * h + j) * nc + o] = (double)v.p[j];
+    }
+}
+
+template <class T>
+__global__ void k_scalar_out(int nc, const int* __restrict__ new2old, const T* __restrict__ a, double* __restrict__ out) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    out[new2old[c]] = (double)a[c];
+}
+
+// Sum of squares of the residual per variable, FP64, deterministic two-level reduction.
+template <class T>
+__global__ void __launch_bounds__(256) k_res_norm_partial(int nc, const Q4<T>* __restrict__ R, double* __restrict__ part) {
+    __shared__ double sh[4][256];
+    double acc[4] = {0, 0, 0, 0};
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        const Q4<T> r = R[c];
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[j] += (double)r.p[j] * (double)r.p[j];
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j++) sh[j][threadIdx.x] = acc[j];
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s)
+#pragma unroll
+            for (int j = 0; j < 4; j++) sh[j][threadIdx.x] += sh[j][threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int j = 0; j < 4; j++) part[4 * blockIdx.x + j] = sh[j][0];
+}
+
+}  // namespace fv2d

@@ -199,3 +199,236 @@ def channel_bump_quads(nx: int = 128, ny: int = 64, length: float = 3.0, height:
     add(pid(ii + 1, jj), pid(ii, jj), cid(ii, jj - 1), cid(ii, jj))
     cat = lambda L: np.concatenate([np.asarray(a).reshape(-1) for a in L]).astype(np.int32)  # noqa: E731
     return Grid(x, y, cat(P1), cat(P2), cat(C1), cat(C2), nx * ny, f"channel_bump_{nx}x{ny}")
+
+
+# --------------------------------------------------------------------------- Voronoi meshes
+def _voronoi_grid(seeds: np.ndarray, ghosts: np.ndarray, ghost_code: np.ndarray, name: str,
+                  vertex_map=None, wall_angle_center=None) -> Grid:
+    """Polygonal mesh from the Voronoi diagram of ``seeds`` closed by mirror ``ghosts``.
+
+    A ridge between two seeds is an interior face; a ridge between a seed and a ghost is a
+    boundary face with the ghost's file code (0 -> BC1, -1 -> BC2); ghost-ghost ridges are dropped.
+    ``vertex_map`` maps Voronoi vertices (and seeds) into the physical domain.  BC1 faces are
+    written first (ordered by angle about ``wall_angle_center`` when given), then BC2 faces, then
+    interior faces; BC1 wall points come first.
+    """
+    from scipy.spatial import Voronoi
+
+    n = seeds.shape[0]
+    pts = np.concatenate([seeds, ghosts])
+    vor = Voronoi(pts)
+    rp = vor.ridge_points.astype(np.int64)
+    rv = np.asarray(vor.ridge_vertices, dtype=np.int64)
+    a_in, b_in = rp[:, 0] < n, rp[:, 1] < n
+    keep = a_in | b_in
+    rp, rv = rp[keep], rv[keep]
+    a_in, b_in = a_in[keep], b_in[keep]
+    if np.any(rv < 0):
+        raise RuntimeError(f"{name}: an interior cell is unbounded (ghost layer too thin)")
+    V = vor.vertices.copy()
+    # merge (near-)coincident vertices left by co-circular seeds: drop zero-length ridges
+    seglen = np.hypot(*(V[rv[:, 1]] - V[rv[:, 0]]).T)
+    scale = np.median(seglen)
+    short = seglen < 1e-9 * scale
+    if np.any(short):
+        parent = np.arange(V.shape[0])
+
+        def find(u):
+            while parent[u] != u:
+                parent[u] = parent[parent[u]]
+                u = parent[u]
+            return u
+
+        for u, w in rv[short]:
+            ru, rw = find(u), find(w)
+            if ru != rw:
+                parent[max(ru, rw)] = min(ru, rw)
+        root = np.array([find(u) for u in range(V.shape[0])])
+        rv = root[rv]
+        ok = rv[:, 0] != rv[:, 1]
+        rp, rv, a_in, b_in = rp[ok], rv[ok], a_in[ok], b_in[ok]
+    if vertex_map is not None:
+        V = vertex_map(V)
+        seeds_m = vertex_map(seeds)
+    else:
+        seeds_m = seeds
+    interior = a_in & b_in
+    c_in = np.where(a_in, rp[:, 0], rp[:, 1])                 # the seed side of a boundary ridge
+    c_gh = np.where(a_in, rp[:, 1], rp[:, 0]) - n
+    code = np.where(interior, 1, ghost_code[np.clip(c_gh, 0, None)])
+    c1 = np.where(interior, np.minimum(rp[:, 0], rp[:, 1]), c_in)
+    c2 = np.where(interior, np.maximum(rp[:, 0], rp[:, 1]), -1)
+    # orientation: c1 on the left of p1 -> p2
+    p1, p2 = rv[:, 0].copy(), rv[:, 1].copy()
+    A, B, S = V[p1], V[p2], seeds_m[c1]
+    cross = (B[:, 0] - A[:, 0]) * (S[:, 1] - A[:, 1]) - (B[:, 1] - A[:, 1]) * (S[:, 0] - A[:, 0])
+    flip = cross < 0
+    p1[flip], p2[flip] = p2[flip], p1[flip]
+    # face order: BC1, BC2, interior
+    is_bc1 = (~interior) & (code == 0)
+    is_bc2 = (~interior) & (code == -1)
+    key = np.zeros(len(p1))
+    if wall_angle_center is not None:
+        mid = 0.5 * (V[p1] + V[p2])
+        key = np.arctan2(mid[:, 1] - wall_angle_center[1], mid[:, 0] - wall_angle_center[0])
+    o1 = np.nonzero(is_bc1)[0]
+    o1 = o1[np.argsort(key[o1], kind="stable")]
+    order = np.concatenate([o1, np.nonzero(is_bc2)[0], np.nonzero(interior)[0]])
+    p1, p2, c1, c2 = p1[order], p2[order], c1[order], c2[order]
+    file_c2 = np.where(c2 >= 0, c2 + 1, 0)
+    nb1 = len(o1)
+    file_c2[nb1:nb1 + int(is_bc2.sum())] = -1
+    file_c2[:nb1] = 0
+    # every cell must be a closed polygon: each of its vertices used by exactly two of its faces
+    cnt = np.bincount(c1, minlength=n) + np.bincount(c2[c2 >= 0], minlength=n)
+    if cnt.min() < 3:
+        raise RuntimeError(f"{name}: a cell has fewer than 3 faces")
+    inc_c = np.concatenate([c1, c1, c2[c2 >= 0], c2[c2 >= 0]])
+    inc_v = np.concatenate([p1, p2, p1[c2 >= 0], p2[c2 >= 0]])
+    pair = np.unique(inc_c * np.int64(V.shape[0]) + inc_v, return_counts=True)[1]
+    if np.any(pair != 2):
+        raise RuntimeError(f"{name}: open cell polygon after vertex merging")
+    # compact points; BC1 wall points first (in face order), then the rest by first use
+    used_order = np.concatenate([np.stack([p1[:nb1], p2[:nb1]], 1).reshape(-1), np.stack([p1, p2], 1).reshape(-1)])
+    _, first = np.unique(used_order, return_index=True)
+    uniq = used_order[np.sort(first)]
+    remap = -np.ones(V.shape[0], np.int64)
+    remap[uniq] = np.arange(len(uniq))
+    X = V[uniq]
+    return Grid(X[:, 0].copy(), X[:, 1].copy(), (remap[p1] + 1).astype(np.int32), (remap[p2] + 1).astype(np.int32),
+                (c1 + 1).astype(np.int32), file_c2.astype(np.int32), n, name)
+
+
+def _mirror_box(p: np.ndarray, h: np.ndarray, x0, x1, y0, y1, band=4.0):
+    """Mirror images of points within ``band*h`` of the edges (and corners) of a box."""
+    out = []
+    nearL, nearR = p[:, 0] - x0 < band * h, x1 - p[:, 0] < band * h
+    nearB, nearT = p[:, 1] - y0 < band * h, y1 - p[:, 1] < band * h
+    for m, fx, fy in ((nearL, 1, 0), (nearR, 2, 0), (nearB, 0, 1), (nearT, 0, 2),
+                      (nearL & nearB, 1, 1), (nearL & nearT, 1, 2), (nearR & nearB, 2, 1), (nearR & nearT, 2, 2)):
+        q = p[m].copy()
+        if fx == 1: q[:, 0] = 2 * x0 - q[:, 0]
+        if fx == 2: q[:, 0] = 2 * x1 - q[:, 0]
+        if fy == 1: q[:, 1] = 2 * y0 - q[:, 1]
+        if fy == 2: q[:, 1] = 2 * y1 - q[:, 1]
+        out.append(q)
+    return np.concatenate(out) if out else np.zeros((0, 2))
+
+
+def _ring_seeds(h_of_r, r_wall, r_max, rng, jitter):
+    """Jittered rings about the origin with radial and tangential spacing h(r)."""
+    rings = []
+    r = r_wall + 0.5 * h_of_r(r_wall)
+    k = 0
+    while r < r_max:
+        h = h_of_r(r)
+        m = max(8, int(round(2 * np.pi * r / h)))
+        th = (np.arange(m) + 0.5 * (k & 1)) * (2 * np.pi / m)
+        rr = np.full(m, r)
+        if jitter > 0:
+            th = th + rng.uniform(-jitter, jitter, m) * (2 * np.pi / m)
+            rr = rr + rng.uniform(-jitter, jitter, m) * h
+        rings.append(np.stack([rr * np.cos(th), rr * np.sin(th), np.full(m, h)], 1))
+        r += h
+        k += 1
+    return np.concatenate(rings)
+
+
+def voronoi_cylinder(target_cells: int = 1_000_000, seed: int = 0, box=(40.0, 20.0), diameter: float = 1.0,
+                     h_wall: float = 0.005, h_far: float = 0.1, jitter: float = 0.2) -> Grid:
+    """Polygonal Voronoi mesh of a box with a circular cylinder at its centre.
+
+    Seeds lie on jittered rings (seeded RNG) whose spacing grows linearly from ``h_wall`` at the
+    cylinder to ``h_far`` far away; the growth rate is calibrated so the mesh has about
+    ``target_cells`` cells.  Cylinder faces (mirror seeds inside the cylinder) are BC1, box faces
+    are BC2.  Cells have 3-9 sides.
+    """
+    W, H = box
+    R = 0.5 * diameter
+    x0, x1, y0, y1 = -W / 2, W / 2, -H / 2, H / 2
+    r_max = float(np.hypot(W / 2, H / 2)) + h_far
+
+    def count(g):
+        hr = lambda r: min(h_far, h_wall + g * (r - R))  # noqa: E731
+        r, k, tot = R + 0.5 * h_wall, 0, 0.0
+        while r < r_max:
+            h = hr(r)
+            m = max(8, int(round(2 * np.pi * r / h)))
+            # fraction of the ring inside the box
+            if r <= min(W, H) / 2:
+                frac = 1.0
+            else:
+                t = np.linspace(0, 2 * np.pi, 256, endpoint=False)
+                frac = np.mean((np.abs(r * np.cos(t)) < W / 2) & (np.abs(r * np.sin(t)) < H / 2))
+            tot += m * frac
+            r += h
+            k += 1
+        return tot
+
+    lo, hi = 1e-5, 1.0
+    for _ in range(40):
+        mid = np.sqrt(lo * hi)
+        if count(mid) > target_cells:
+            lo = mid
+        else:
+            hi = mid
+    g = np.sqrt(lo * hi)
+    rng = np.random.default_rng(seed)
+    hr = lambda r: min(h_far, h_wall + g * (r - R))  # noqa: E731
+    s = _ring_seeds(hr, R, r_max, rng, jitter)
+    h = s[:, 2]
+    inside = (s[:, 0] > x0 + 0.3 * h) & (s[:, 0] < x1 - 0.3 * h) & (s[:, 1] > y0 + 0.3 * h) & (s[:, 1] < y1 - 0.3 * h)
+    s = s[inside]
+    p, h = s[:, :2], s[:, 2]
+    rad = np.hypot(p[:, 0], p[:, 1])
+    near = rad < R + 4 * h
+    cyl_ghost = p[near] * ((2 * R - rad[near]) / rad[near])[:, None]
+    box_ghost = _mirror_box(p, h, x0, x1, y0, y1)
+    ghosts = np.concatenate([cyl_ghost, box_ghost])
+    code = np.concatenate([np.zeros(len(cyl_ghost), np.int64), -np.ones(len(box_ghost), np.int64)])
+    return _voronoi_grid(p, ghosts, code, f"voronoi_cylinder_{len(p)}", wall_angle_center=(0.0, 0.0))
+
+
+def voronoi_bump_channel(target_cells: int = 4_000_000, seed: int = 0, length: float = 4.0, height: float = 1.0,
+                         thickness: float = 0.1, bump=(1.5, 2.5), jitter: float = 0.25) -> Grid:
+    """Polygonal Voronoi mesh of a channel with a circular-arc bump on the lower wall.
+
+    Seeds form a jittered hexagonal lattice (seeded RNG) in the straight channel
+    [0, length] x [0, height], closed by mirror seeds across its four sides; Voronoi vertices are
+    then mapped to the bumped channel by y -> yw(x) + (height - yw(x)) y / height.  Lower and upper
+    walls are BC1 (written bottom first), inlet and outlet are BC2.
+    """
+    area = length * height
+    hx = np.sqrt(area / target_cells / (np.sqrt(3) / 2))
+    hy = hx * np.sqrt(3) / 2
+    ny = max(2, int(round(height / hy)))
+    hy = height / ny
+    nx = max(2, int(round(length / hx)))
+    hx = length / nx
+    rng = np.random.default_rng(seed)
+    j = np.arange(ny)
+    i = np.arange(nx)
+    X = (i[None, :] + 0.5 + 0.5 * ((j[:, None] & 1) - 0.5)) * hx
+    Y = np.broadcast_to((j[:, None] + 0.5) * hy, X.shape)
+    p = np.stack([X.reshape(-1), Y.reshape(-1)], 1)
+    p = p + rng.uniform(-jitter, jitter, p.shape) * np.array([hx, hy])
+    p[:, 0] = np.clip(p[:, 0], 0.05 * hx, length - 0.05 * hx)
+    hh = np.full(len(p), max(hx, hy))
+    gL = p[p[:, 0] < 4 * hh[0]] * np.array([-1, 1])
+    gR = p[p[:, 0] > length - 4 * hh[0]] * np.array([-1, 1]) + np.array([2 * length, 0])
+    gB = p[p[:, 1] < 4 * hh[0]] * np.array([1, -1])
+    gT = p[p[:, 1] > height - 4 * hh[0]] * np.array([1, -1]) + np.array([0, 2 * height])
+    corners = []
+    for cx, sx in ((0.0, -1), (length, -1)):
+        for cy, sy in ((0.0, -1), (height, -1)):
+            m = (np.abs(p[:, 0] - cx) < 4 * hh[0]) & (np.abs(p[:, 1] - cy) < 4 * hh[0])
+            corners.append(np.stack([2 * cx - p[m, 0], 2 * cy - p[m, 1]], 1))
+    ghosts = np.concatenate([gB, gT, gL, gR] + corners)
+    code = np.concatenate([np.zeros(len(gB) + len(gT), np.int64),
+                           -np.ones(len(gL) + len(gR) + sum(len(c) for c in corners), np.int64)])
+
+    def vmap(v):
+        yw = bump_wall(v[:, 0], bump[0], bump[1], thickness) if thickness > 0 else np.zeros(len(v))
+        return np.stack([v[:, 0], yw + (height - yw) * v[:, 1] / height], 1)
+
+    return _voronoi_grid(p, ghosts, code, f"voronoi_bump_{len(p)}", vertex_map=vmap)
