@@ -3,7 +3,10 @@
 Workload (default): 2-D Navier-Stokes flow around a circular cylinder (D = 1, centred in a
 40 x 20 box) on a ~1M-cell polygonal Voronoi mesh with jittered seeds graded from 0.005 at the
 wall to 0.1 far away; Re = 100, Mach 0.2, Pr = 0.72, NO_SLIP_WALL cylinder, FREESTREAM box,
-second order with the squeeze limiter, LOCAL time step at CFL 0.9, FP64 plain path.
+second order with the squeeze limiter, LOCAL time step, FP64 plain path.  The time step runs at
+CFL 0.5: the reference scheme itself (checked with the bit-exact oracle) diverges at the cylinder
+wall within 5-25 iterations for any CFL from 0.6 to 0.9 on this mesh; the work per iteration does
+not depend on the CFL number.
 One step = one SSP-RK3 iteration = 3 x num_cells cell-stage updates.  The mesh (~0.5 GB of
 device arrays) is larger than the 129 MB L2, so no flush is needed between steps.
 
@@ -32,6 +35,7 @@ sys.path.insert(0, ROOT)
 import __graft_entry__ as entry  # noqa: E402
 
 METRIC = "cell-stage updates/s"
+WORKLOAD_CFL = 0.5
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
 
@@ -41,7 +45,7 @@ def workload_case(pkg, cells):
     u = mg.mach_speed(0.2)
     mu = 1.225 * u * 1.0 / 100.0           # Re = rho u D / mu = 100
     case = dict(mg.DEFAULT_CASE, eqn="NS", mu=mu, Pr=0.72, u=u, v=0.0, limiter="SQUEEZE", time_step_type="LOCAL",
-                CFL=0.9, BC1="NO_SLIP_WALL", BC2="FREESTREAM", solution_poly_order=1)
+                CFL=WORKLOAD_CFL, BC1="NO_SLIP_WALL", BC2="FREESTREAM", solution_poly_order=1)
     return case
 
 
@@ -308,7 +312,7 @@ def run_gpu_arm(args):
                 "vs_baseline": None, "dtype": "f64" if prec == pkg.FP64 else "f32", "data": "synthetic",
                 "config": {"workload": "ns_cylinder_voronoi", "cells": N, "faces": F, "boundary_faces": Nb,
                            "max_sides": max(grid.sides_histogram()), "precision": args.precision,
-                           "re": 100, "mach": 0.2, "limiter": "SQUEEZE", "dt": "LOCAL", "cfl": 0.9,
+                           "re": 100, "mach": 0.2, "limiter": "SQUEEZE", "dt": "LOCAL", "cfl": WORKLOAD_CFL,
                            "l2": "working set > L2 (no flush)", "parallelism": f"{ws} replicas" if ws > 1 else "single GPU",
                            "mesh_gen_s": round(t_mesh, 1)},
                 "clocks": clk, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": gpu_launches,

@@ -288,6 +288,16 @@ def _voronoi_grid(seeds: np.ndarray, ghosts: np.ndarray, ghost_code: np.ndarray,
     pair = np.unique(inc_c * np.int64(V.shape[0]) + inc_v, return_counts=True)[1]
     if np.any(pair != 2):
         raise RuntimeError(f"{name}: open cell polygon after vertex merging")
+    # cell numbering: the cells next to BC1 faces first, in BC1 face order, then the others in seed
+    # order.  With one wall face per wall cell this makes cell number k the owner of wall face k,
+    # which is the cell the reference's NO_SLIP_WALL gradient ghost reads (cell_gradient.cpp:63-66).
+    first_wall = np.unique(c1[:nb1], return_index=True)[1]
+    wall_cells = c1[:nb1][np.sort(first_wall)]
+    rest = np.setdiff1d(np.arange(n), wall_cells, assume_unique=False)
+    cell_new = np.empty(n, np.int64)
+    cell_new[np.concatenate([wall_cells, rest])] = np.arange(n)
+    c1 = cell_new[c1]
+    file_c2 = np.where(file_c2 > 0, cell_new[np.maximum(file_c2 - 1, 0)] + 1, file_c2)
     # compact points; BC1 wall points first (in face order), then the rest by first use
     used_order = np.concatenate([np.stack([p1[:nb1], p2[:nb1]], 1).reshape(-1), np.stack([p1, p2], 1).reshape(-1)])
     _, first = np.unique(used_order, return_index=True)
@@ -315,9 +325,11 @@ def _mirror_box(p: np.ndarray, h: np.ndarray, x0, x1, y0, y1, band=4.0):
     return np.concatenate(out) if out else np.zeros((0, 2))
 
 
-def _ring_seeds(h_of_r, r_wall, r_max, rng, jitter):
-    """Jittered rings about the origin with radial and tangential spacing h(r)."""
+def _ring_seeds(h_of_r, r_wall, r_max, rng, jitter_max):
+    """Jittered rings about the origin with radial and tangential spacing h(r).  The first ring
+    (next to the wall) is regular, so each of its cells owns exactly one wall face."""
     rings = []
+    jitter = 0.0
     r = r_wall + 0.5 * h_of_r(r_wall)
     k = 0
     while r < r_max:
@@ -329,6 +341,7 @@ def _ring_seeds(h_of_r, r_wall, r_max, rng, jitter):
             th = th + rng.uniform(-jitter, jitter, m) * (2 * np.pi / m)
             rr = rr + rng.uniform(-jitter, jitter, m) * h
         rings.append(np.stack([rr * np.cos(th), rr * np.sin(th), np.full(m, h)], 1))
+        jitter = jitter_max                      # the ring next to the wall is not jittered
         r += h
         k += 1
     return np.concatenate(rings)
