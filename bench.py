@@ -77,7 +77,7 @@ class Clocks:
             os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                                          "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+                                          "-lms", "100"], stdout=self.fh, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
 
@@ -153,6 +153,16 @@ def roofline(kt, N, F, ninc, Nb, s, ns, squeeze, peak):
                  "frac": round(achieved / peak, 4), "traffic": None, "kernel": dom,
                  "kernel_avg_ms": round(d["avg_ms"], 4), "bytes_per_launch": int(d["bytes"]),
                  "share": {k: round(v["total_ms"] / tot, 3) for k, v in per.items()}}, per
+
+
+def ncu_traffic(precision, kernel, N, F):
+    """DRAM bytes of one launch of `kernel` from the committed ncu capture, scaled by units."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as fh:
+            t = json.load(fh)[precision][kernel]
+        return int(t["bytes"] / t["units"] * (N if t["per"] == "cells" else F))
+    except Exception:
+        return None
 
 
 def peaks():
@@ -280,6 +290,7 @@ def run_gpu_arm(args):
     peak, peak_kind = peaks()
     dom, roof, per = roofline(kt, N, F, ninc, Nb, s_bytes, True, True, peak)
     roof["peak_source"] = f"{peak_kind} hbm_gbs"
+    roof["traffic"] = ncu_traffic(args.precision, dom, N, F)
     launches = sum(v[1] for k, v in kt.items() if k in ("k_gradient", "k_face", "k_update"))
     gpu_launches = 3 * 3 * args.steps
 
@@ -330,7 +341,7 @@ def run_gpu_arm(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cells", type=int, default=1_000_000)
