@@ -42,6 +42,7 @@ def _units():
         # the FP64 engine must not contract a*b+c: bit-identical with the reference
         ("fv2d_fp64.cu", [nvcc] + common + ["-fmad=false"]),
         ("fv2d_fp32.cu", [nvcc] + common),
+        ("fv2d_noalloc.cu", [nvcc] + common + ["-fmad=false"]),
     ]
 
 

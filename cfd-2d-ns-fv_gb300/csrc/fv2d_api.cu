@@ -26,6 +26,13 @@ struct fv2d_mesh {
 
 namespace {
 thread_local std::string g_err;
+}  // namespace
+
+namespace fv2d {
+void set_global_error(const std::string& msg) { g_err = msg; }
+}  // namespace fv2d
+
+namespace {
 
 int fail(int code, const std::string& msg) {
     g_err = msg;

@@ -152,6 +152,44 @@ long long fv2d_device_bytes(fv2d_handle* h);
 
 const char* fv2d_last_error(fv2d_handle* h);   /* h may be NULL: last creation error */
 
+/* ---- residual without allocation ----------------------------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device memory: a host
+ * application whose own allocator has reserved the GPU's memory up front (a cudaMalloc here would
+ * fail or fragment its pool), or a latency-critical thread that must not call cudaMalloc/cudaFree
+ * because they can synchronise the whole device.  The caller passes every input and output as
+ * device memory it already owns; the call computes the FIRST-ORDER residual (res() with
+ * solution_poly_order = 0, src/solver/res.cpp:21: boundary ghosts, Rusanov flux, gather / volume;
+ * no viscous flux, as in the reference at first order) and allocates nothing.
+ *
+ * Its per-face scratch is a static device array of FV2D_NOALLOC_MAX_FACES x 4 doubles (8 MiB),
+ * held by every GPU that loads this library until the process exits; meshes with more faces are
+ * rejected with FV2D_ERR_ARG (use fv2d_create / fv2d_stage for those).  The first call on each
+ * device looks up that array's device address with the device current; make that first call
+ * before any stream capture.  The scratch is fully rewritten before it is read, so no state
+ * carries over between calls, but all calls share it: calls that overlap on the GPU (other
+ * streams, other host threads on the same device) race and must be serialised by the caller.
+ * The kernels are launched on `stream` (a cudaStream_t, NULL = legacy default stream) and the call
+ * returns without waiting; errors: fv2d_last_error(NULL).
+ *
+ * Mesh arrays use the reference's numbering and codes (0-based; face_cell2 < 0 is the BC code
+ * -1..-4), cell_faces holds (face id << 1) | side (side 1 when the cell is face_cell2) in
+ * ascending face id per cell, which reproduces the reference's summation order; q and r are SoA
+ * p1..p4 blocks of num_cells doubles.  From the case only gamma and the [init] state are read. */
+#define FV2D_NOALLOC_MAX_FACES 262144
+typedef struct fv2d_noalloc_mesh {
+    int num_cells, num_faces;
+    const int* face_cell1;          /* device [num_faces]                       */
+    const int* face_cell2;          /* device [num_faces]                       */
+    const double* face_nx;          /* device [num_faces]                       */
+    const double* face_ny;          /* device [num_faces]                       */
+    const double* face_area;        /* device [num_faces]                       */
+    const int* cell_face_offsets;   /* device [num_cells + 1]                   */
+    const int* cell_faces;          /* device [cell_face_offsets[num_cells]]    */
+    const double* cell_vol;         /* device [num_cells]                       */
+} fv2d_noalloc_mesh;
+int fv2d_residual_noalloc(const fv2d_noalloc_mesh* mesh, const fv2d_case* cs, const double* q, double* r,
+                          void* stream);
+
 /* Field ids for fv2d_get_field / fv2d_mesh_get (same numbering as the oracle's interface).     */
 enum fv2d_field {
     FV2D_F_QBAR = 0,        /* 4N  Qbar                                                  */
