@@ -6,5 +6,5 @@ The directory name contains dashes, so load it with ``load_package()`` from the 
 and import it under the name ``fv2d_gb300`` through importlib.
 """
 from . import build, meshgen  # noqa: F401
-from .fv2d import (FP32, FP64, Case, Fv2dError, HostMesh, Solver, case_from_dict, library,  # noqa: F401
+from .fv2d import (FP32, FP64, Batch, Case, Fv2dError, HostMesh, Solver, case_from_dict, library,  # noqa: F401
                    read_inputs)

@@ -8,6 +8,7 @@
 
 #include "fv2d_gpu.h"
 #include "fv2d_host.h"
+#include "fv2d_batch.h"
 #include "fv2d_solver.h"
 
 namespace fv2d {
@@ -22,6 +23,11 @@ struct fv2d_handle {
 
 struct fv2d_mesh {
     fv2d::HostMesh m;
+};
+
+struct fv2d_batch {
+    std::unique_ptr<fv2d::Batch> b;
+    int precision = FV2D_FP32;
 };
 
 namespace {
@@ -250,4 +256,103 @@ const char* fv2d_last_error(fv2d_handle* h) {
     return g_err.c_str();
 }
 
+
+// ---- batch -------------------------------------------------------------------------------------
+#define FV2D_BH(b) if (!(b) || !(b)->b) return fail(FV2D_ERR_ARG, "null batch")
+#define FV2D_BRET(b, expr) do { int rc_ = (expr); if (rc_) g_err = (b)->b->err_; return rc_; } while (0)
+
+int fv2d_batch_create(long long max_cells, long long max_faces, int max_solves, int precision, fv2d_batch** out) {
+    if (!out) return fail(FV2D_ERR_ARG, "null output");
+    *out = nullptr;
+    if (precision != FV2D_FP64 && precision != FV2D_FP32) return fail(FV2D_ERR_ARG, "precision must be FV2D_FP64 or FV2D_FP32");
+    int rc = check_device();
+    if (rc) return rc;
+    auto b = std::make_unique<fv2d_batch>();
+    b->precision = precision;
+    b->b.reset(precision == FV2D_FP64 ? fv2d::make_batch_fp64() : fv2d::make_batch_fp32());
+    rc = b->b->init(max_cells, max_faces, max_solves);
+    if (rc) return fail(rc, b->b->err_);
+    *out = b.release();
+    return FV2D_OK;
+}
+
+void fv2d_batch_destroy(fv2d_batch* b) { delete b; }
+
+int fv2d_batch_footprint(const fv2d_mesh_desc* d, int precision, long long* bytes) {
+    if (!d || !bytes) return fail(FV2D_ERR_ARG, "null argument");
+    if (!d->face_cell2 || d->num_faces <= 0 || d->num_cells <= 0) return fail(FV2D_ERR_ARG, "empty mesh");
+    long long nb = 0;
+    for (int f = 0; f < d->num_faces; f++) nb += d->face_cell2[f] <= 0;
+    fv2d::batch_footprint(precision, d->num_cells, d->num_faces, 2LL * d->num_faces - nb, bytes);
+    return FV2D_OK;
+}
+
+int fv2d_batch_add(fv2d_batch* b, const fv2d_mesh_desc* desc, const fv2d_case* cs, int* solve_id) {
+    FV2D_BH(b);
+    if (!solve_id) return fail(FV2D_ERR_ARG, "null output");
+    int rc = check_case(cs);
+    if (rc) return rc;
+    FV2D_BRET(b, b->b->add(desc, cs, solve_id));
+}
+
+int fv2d_batch_remove(fv2d_batch* b, int solve_id) { FV2D_BH(b); FV2D_BRET(b, b->b->remove(solve_id)); }
+int fv2d_batch_step(fv2d_batch* b, int iterations) { FV2D_BH(b); FV2D_BRET(b, b->b->step(iterations)); }
+
+int fv2d_batch_norms(fv2d_batch* b, int* ids, double* norms4, int* iterations, int max, int* n) {
+    FV2D_BH(b);
+    if (!ids || !norms4 || !n) return fail(FV2D_ERR_ARG, "null output");
+    FV2D_BRET(b, b->b->norms(ids, norms4, iterations, max, n));
+}
+
+int fv2d_batch_get_state(fv2d_batch* b, int solve_id, double* q) {
+    FV2D_BH(b);
+    if (!q) return fail(FV2D_ERR_ARG, "null output");
+    FV2D_BRET(b, b->b->get_state(solve_id, q));
+}
+
+int fv2d_batch_synchronize(fv2d_batch* b) { FV2D_BH(b); FV2D_BRET(b, b->b->synchronize()); }
+
+int fv2d_batch_set_tuning(fv2d_batch* b, int block, const int* tile_mult3, const int* bucket_edges2) {
+    FV2D_BH(b);
+    fv2d::BatchTuning t = b->b->tuning();
+    t.block = block;
+    if (tile_mult3) for (int i = 0; i < 3; i++) t.tile_mult[i] = tile_mult3[i];
+    if (bucket_edges2) for (int i = 0; i < 2; i++) t.bucket_edges[i] = bucket_edges2[i];
+    FV2D_BRET(b, b->b->set_tuning(t));
+}
+
+int fv2d_batch_get_tuning(fv2d_batch* b, int* block, int* tile_mult3, int* bucket_edges2) {
+    FV2D_BH(b);
+    const fv2d::BatchTuning t = b->b->tuning();
+    if (block) *block = t.block;
+    if (tile_mult3) for (int i = 0; i < 3; i++) tile_mult3[i] = t.tile_mult[i];
+    if (bucket_edges2) for (int i = 0; i < 2; i++) bucket_edges2[i] = t.bucket_edges[i];
+    return FV2D_OK;
+}
+
+int fv2d_batch_usage(fv2d_batch* b, long long* out8) {
+    FV2D_BH(b);
+    if (!out8) return fail(FV2D_ERR_ARG, "null output");
+    FV2D_BRET(b, b->b->usage(out8));
+}
+
+int fv2d_batch_set_kernel_timing(fv2d_batch* b, int enable) { FV2D_BH(b); FV2D_BRET(b, b->b->set_timing(enable)); }
+
+int fv2d_batch_kernel_times(fv2d_batch* b, double* ms3, int* launches3) {
+    FV2D_BH(b);
+    if (!ms3 || !launches3) return fail(FV2D_ERR_ARG, "null output");
+    FV2D_BRET(b, b->b->kernel_times(ms3, launches3));
+}
+
+void* fv2d_batch_stream(fv2d_batch* b) { return (b && b->b) ? b->b->stream() : nullptr; }
+
 }  // extern "C"
+
+namespace fv2d {
+void batch_footprint(int precision, long long cells, long long faces, long long incs, long long* bytes) {
+    const long long s = precision == FV2D_FP64 ? 8 : 4;
+    const long long cell = (precision == FV2D_FP64 ? 9 : 11) * 4 * s + 3 * s + 24 + 4;   // Q[3], G[3], (D, lo), dt, S, vol, LSQ, offsets
+    const long long face = 3 * 4 + 14 * s + 4 * s + s;        // ids, geometry, contribution, spectral term
+    *bytes = (cells + 1) * cell + faces * face + incs * 8;
+}
+}  // namespace fv2d

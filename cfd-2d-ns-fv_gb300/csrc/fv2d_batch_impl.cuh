@@ -1,0 +1,609 @@
+// Batched engine: many independent solves in one device arena.
+//
+// Every solve owns a contiguous cell range, face range and incidence range of the arena's
+// capacity-sized arrays; its arrays hold ARENA ids (cell, face and incidence ids shifted by the
+// range starts), so the per-element device functions of the single-solve kernels run unchanged.
+// Work is described by tile lists in device memory (tile = up to `block * mult` cells or faces of
+// one solve); each stage kernel is a persistent grid looping over its tiles, loads the solve's
+// parameters into shared memory once per tile and applies the same per-element code.  One
+// iteration (3 stages x 3 kernels + 2 memsets) is captured in a CUDA graph; since the graph reads
+// the tile lists and parameter table from device memory, solves can join and leave between
+// iterations without re-capturing.  Per-solve reductions (GLOBAL dt maximum, residual L2 sums)
+// use one atomic per tile.
+#pragma once
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <vector>
+
+#include "fv2d_batch.h"
+#include "fv2d_kernels.cuh"
+
+namespace fv2d {
+
+template <class T>
+struct SolveParams {
+    Consts<T> k;
+    int order2, ns, squeeze, global_dt;
+    int fresh, init_prims, pad0, pad1;
+};
+
+struct Tile {
+    int sid, start, count, pad;
+};
+
+template <class T>
+__device__ __forceinline__ T block_sum(T v, T* red) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[w] = v;
+    __syncthreads();
+    T s = T(0);
+    if (threadIdx.x == 0)
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) s += red[i];
+    return s;   // valid in thread 0
+}
+
+template <class T>
+__device__ __forceinline__ T block_max_t(T v, T* red) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max2(v, __shfl_xor_sync(0xffffffffu, v, o));
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[w] = v;
+    __syncthreads();
+    T s = T(0);
+    if (threadIdx.x == 0)
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) s = max2(s, red[i]);
+    return s;   // valid in thread 0
+}
+
+template <class T>
+__global__ void __launch_bounds__(512)
+kb_gradient(const Tile* __restrict__ tiles, const int* __restrict__ ntiles, DevMesh<T> m,
+            const SolveParams<T>* __restrict__ P, const Q4<T>* __restrict__ Qin, const Q4<T>* __restrict__ Qprev,
+            const Q4<T>* __restrict__ Gprev, Q4<T>* __restrict__ Gout) {
+    __shared__ SolveParams<T> sp;
+    __shared__ Tile st;
+    const int nt = *ntiles;
+    for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+        if (threadIdx.x == 0) { st = tiles[t]; sp = P[st.sid]; }
+        __syncthreads();
+        if (sp.order2) {
+            if (sp.squeeze) {
+                for (int e = threadIdx.x; e < st.count; e += blockDim.x)
+                    gradient_cell<T, true>(st.start + e, m, Qin, Qprev, Gprev, Gout, sp.k, sp.fresh, sp.init_prims);
+            } else {
+                for (int e = threadIdx.x; e < st.count; e += blockDim.x)
+                    gradient_cell<T, false>(st.start + e, m, Qin, Qprev, Gprev, Gout, sp.k, sp.fresh, sp.init_prims);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <class T, bool LAST>
+__global__ void __launch_bounds__(512)
+kb_face(const Tile* __restrict__ tiles, const int* __restrict__ ntiles, DevMesh<T> m,
+        const SolveParams<T>* __restrict__ P, const Q4<T>* __restrict__ Qin, const Q4<T>* __restrict__ G,
+        Q4<T>* __restrict__ tout, T* __restrict__ sout) {
+    __shared__ SolveParams<T> sp;
+    __shared__ Tile st;
+    const int nt = *ntiles;
+    for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+        if (threadIdx.x == 0) { st = tiles[t]; sp = P[st.sid]; }
+        __syncthreads();
+        if (!sp.order2) {
+            for (int e = threadIdx.x; e < st.count; e += blockDim.x)
+                face_flux<T, false, false, LAST>(st.start + e, m, Qin, G, tout, sout, sp.k, sp.init_prims);
+        } else if (sp.ns) {
+            for (int e = threadIdx.x; e < st.count; e += blockDim.x)
+                face_flux<T, true, true, LAST>(st.start + e, m, Qin, G, tout, sout, sp.k, sp.init_prims);
+        } else {
+            for (int e = threadIdx.x; e < st.count; e += blockDim.x)
+                face_flux<T, true, false, LAST>(st.start + e, m, Qin, G, tout, sout, sp.k, sp.init_prims);
+        }
+        __syncthreads();
+    }
+}
+
+template <class T, int STAGE>
+__global__ void __launch_bounds__(512)
+kb_update(const Tile* __restrict__ tiles, const int* __restrict__ ntiles, DevMesh<T> m, SolveParams<T>* P,
+          const Q4<T>* __restrict__ tface, const T* __restrict__ sface, Q4<T>* __restrict__ Qn, Q4<T>* __restrict__ Q1,
+          Q4<T>* __restrict__ Q2, T* __restrict__ dt, T* __restrict__ S, T* __restrict__ smax, double* __restrict__ res2,
+          int* __restrict__ flags, Q4<T>* __restrict__ D, Q4<T>* __restrict__ Qlo) {
+    __shared__ SolveParams<T> sp;
+    __shared__ Tile st;
+    __shared__ double redd[32];
+    __shared__ T redt[32];
+    const int nt = *ntiles;
+    for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+        if (threadIdx.x == 0) { st = tiles[t]; sp = P[st.sid]; }
+        __syncthreads();
+        const T sm = (STAGE == 0 && sp.global_dt) ? smax[st.sid] : T(0);
+        T mx = T(0);
+        double acc[4] = {0, 0, 0, 0};
+        for (int e = threadIdx.x; e < st.count; e += blockDim.x) {
+            T r[4];
+            const T sn = update_cell<T, STAGE>(st.start + e, m, tface, sface, Qn, Q1, Q2, dt, S, sm, nullptr,
+                                               flags + st.sid, sp.k, sp.global_dt, r, D, Qlo);
+            if (STAGE == 2) {
+                mx = max2(mx, sn);
+#pragma unroll
+                for (int j = 0; j < 4; j++) acc[j] += (double)r[j] * (double)r[j];
+            }
+        }
+        if (STAGE == 2) {
+            const T bm = block_max_t(mx, redt);
+            if (threadIdx.x == 0) atomic_max_pos(smax + st.sid, bm);
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const double bs = block_sum(acc[j], redd);
+                if (threadIdx.x == 0) atomicAdd(res2 + 4 * st.sid + j, bs);
+            }
+        }
+        if (STAGE == 0 && threadIdx.x == 0) { P[st.sid].fresh = 0; P[st.sid].init_prims = 0; }
+        __syncthreads();
+    }
+}
+
+// First-fit allocator of index ranges with coalescing frees.
+class RangeAlloc {
+public:
+    void reset(long long cap) { cap_ = cap; free_.clear(); if (cap > 0) free_[0] = cap; used_ = 0; }
+    bool alloc(long long n, long long* start) {
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second >= n) {
+                *start = it->first;
+                const long long rest = it->second - n, at = it->first + n;
+                free_.erase(it);
+                if (rest > 0) free_[at] = rest;
+                used_ += n;
+                return true;
+            }
+        }
+        return false;
+    }
+    void release(long long start, long long n) {
+        if (n <= 0) return;
+        used_ -= n;
+        auto it = free_.emplace(start, n).first;
+        auto nx = std::next(it);
+        if (nx != free_.end() && it->first + it->second == nx->first) { it->second += nx->second; free_.erase(nx); }
+        if (it != free_.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) { pv->second += it->second; free_.erase(it); }
+        }
+    }
+    long long used() const { return used_; }
+    long long cap() const { return cap_; }
+private:
+    long long cap_ = 0, used_ = 0;
+    std::map<long long, long long> free_;
+};
+
+#define FV2D_B(call)                                                                              \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess) {                                                                  \
+            err_ = std::string(#call) + ": " + cudaGetErrorString(e_);                            \
+            return e_ == cudaErrorMemoryAllocation ? FV2D_ERR_NOMEM : FV2D_ERR_CUDA;              \
+        }                                                                                         \
+    } while (0)
+
+template <class T>
+class BatchImpl : public Batch {
+    struct Rec {
+        bool active = false;
+        long long c0 = 0, n = 0, f0 = 0, m = 0, i0 = 0, k = 0;
+        std::vector<int> n2o;
+        int iterations = 0;
+    };
+
+public:
+    ~BatchImpl() override {
+        if (graph_) cudaGraphExecDestroy(graph_);
+        for (auto& p : pending_) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
+        for (auto e : free_events_) cudaEventDestroy(e);
+        if (arena_) cudaFree(arena_);
+        if (pin_) cudaFreeHost(pin_);
+        if (stream_) cudaStreamDestroy(stream_);
+    }
+
+    int init(long long max_cells, long long max_faces, int max_solves) override {
+        if (max_cells <= 0 || max_faces <= 0 || max_solves <= 0 || max_cells > (1LL << 30) || max_faces > (1LL << 29)) {
+            err_ = "batch capacity out of range (cells <= 2^30, faces <= 2^29)";
+            return FV2D_ERR_ARG;
+        }
+        Nc_ = max_cells + max_solves;   // one sentinel offset slot per solve
+        Fc_ = max_faces;
+        Ic_ = 2 * max_faces;
+        S_ = max_solves;
+        FV2D_B(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+        size_t off = 0;
+        auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) & ~size_t(255); return o; };
+        const size_t q4 = sizeof(Q4<T>);
+        size_t oq[3], og[3];
+        for (int i = 0; i < 3; i++) oq[i] = take(q4 * Nc_);
+        for (int i = 0; i < 3; i++) og[i] = take(2 * q4 * Nc_);
+        size_t odt = take(sizeof(T) * Nc_), oS = take(sizeof(T) * Nc_), ovol = take(sizeof(T) * Nc_);
+        size_t oixx = take(8 * Nc_), oiyy = take(8 * Nc_), oixy = take(8 * Nc_), ooff = take(4 * Nc_);
+        size_t oinc = take(4 * Ic_), onbr = take(4 * Ic_);
+        size_t ofc1 = take(4 * Fc_), ofc2 = take(4 * Fc_), oqc = take(4 * Fc_);
+        size_t ogeo[14];
+        for (int gI = 0; gI < 14; gI++) ogeo[gI] = take(sizeof(T) * Fc_);
+        size_t ot = take(q4 * Fc_), os = take(sizeof(T) * Fc_);
+        size_t oP = take(sizeof(SolveParams<T>) * S_), osmax = take(sizeof(T) * S_), ores = take(32 * (size_t)S_);
+        size_t oflag = take(4 * (size_t)S_);
+        const bool comp = sizeof(T) == 4;   // FP32: delta-form increments + compensated base state
+        size_t oD = comp ? take(q4 * Nc_) : 0, olo = comp ? take(q4 * Nc_) : 0;
+        tile_cap_ = (int)std::min<long long>((Nc_ + Fc_) / 64 + 4 * (long long)S_ + 16, 1LL << 28);
+        size_t otc = take(sizeof(Tile) * tile_cap_), otf = take(sizeof(Tile) * tile_cap_), ocnt = take(64);
+        bytes_ = off;
+        FV2D_B(cudaMalloc(&arena_, bytes_));
+        char* a = (char*)arena_;
+        for (int i = 0; i < 3; i++) { Q_[i] = (Q4<T>*)(a + oq[i]); G_[i] = (Q4<T>*)(a + og[i]); }
+        dt_ = (T*)(a + odt); S_arr_ = (T*)(a + oS);
+        T* vol = (T*)(a + ovol);
+        double *ixx = (double*)(a + oixx), *iyy = (double*)(a + oiyy), *ixy = (double*)(a + oixy);
+        int *incoff = (int*)(a + ooff), *inc = (int*)(a + oinc), *nbr = (int*)(a + onbr);
+        int *fc1 = (int*)(a + ofc1), *fc2 = (int*)(a + ofc2), *qc = (int*)(a + oqc);
+        for (int gI = 0; gI < 14; gI++) geo_[gI] = (T*)(a + ogeo[gI]);
+        t_ = (Q4<T>*)(a + ot); s_ = (T*)(a + os);
+        P_ = (SolveParams<T>*)(a + oP); smax_ = (T*)(a + osmax); res2_ = (double*)(a + ores); flags_ = (int*)(a + oflag);
+        tc_ = (Tile*)(a + otc); tf_ = (Tile*)(a + otf); cnt_ = (int*)(a + ocnt);
+        D_ = comp ? (Q4<T>*)(a + oD) : nullptr;
+        Qlo_ = comp ? (Q4<T>*)(a + olo) : nullptr;
+        m_.inc_off = incoff; m_.inc = inc; m_.nbr = nbr; m_.fc1 = fc1; m_.fc2 = fc2; m_.qcell = qc;
+        m_.g.nx = geo_[0]; m_.g.ny = geo_[1]; m_.g.area = geo_[2]; m_.g.c1dx = geo_[3]; m_.g.c1dy = geo_[4];
+        m_.g.c2dx = geo_[5]; m_.g.c2dy = geo_[6]; m_.g.dxj = geo_[7]; m_.g.dyj = geo_[8]; m_.g.mx = geo_[9];
+        m_.g.my = geo_[10]; m_.g.lx = geo_[11]; m_.g.ly = geo_[12]; m_.g.dist = geo_[13];
+        m_.Ixx = ixx; m_.Iyy = iyy; m_.Ixy = ixy; m_.vol = vol;
+        FV2D_B(cudaMemsetAsync(arena_, 0, bytes_, stream_));
+        FV2D_B(cudaStreamSynchronize(stream_));
+        cells_.reset(Nc_);
+        faces_.reset(Fc_);
+        incs_.reset(Ic_);
+        recs_.assign(S_, Rec());
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev);
+        compute_grids();
+        return FV2D_OK;
+    }
+
+    int add(const fv2d_mesh_desc* d, const fv2d_case* cs, int* sid_out) override {
+        int sid = -1;
+        for (int i = 0; i < S_; i++) if (!recs_[i].active) { sid = i; break; }
+        if (sid < 0) { err_ = "batch is full (max solves)"; return FV2D_ERR_NOMEM; }
+        HostMesh hm;
+        int rc = build_mesh(d, cs, hm, err_);
+        if (rc) return rc;
+        DeviceLayout L;
+        build_layout(hm, L);
+        Rec r;
+        r.n = hm.nc; r.m = hm.nf; r.k = L.ninc;
+        if (!cells_.alloc(r.n + 1, &r.c0)) { err_ = "batch cell capacity exhausted"; return FV2D_ERR_NOMEM; }
+        if (!faces_.alloc(r.m, &r.f0)) { cells_.release(r.c0, r.n + 1); err_ = "batch face capacity exhausted"; return FV2D_ERR_NOMEM; }
+        if (!incs_.alloc(r.k, &r.i0)) {
+            cells_.release(r.c0, r.n + 1); faces_.release(r.f0, r.m);
+            err_ = "batch incidence capacity exhausted"; return FV2D_ERR_NOMEM;
+        }
+        // shift local ids to arena ids
+        for (auto& v : L.inc_off) v += (int)r.i0;
+        for (auto& v : L.inc) v = (((v >> 1) + (int)r.f0) << 1) | (v & 1);
+        for (auto& v : L.nbr) if (v >= 0) v += (int)r.c0;
+        for (auto& v : L.fc1) v += (int)r.c0;
+        for (auto& v : L.fc2) if (v >= 0) v += (int)r.c0;
+        for (auto& v : L.qcell) if (v >= 0) v += (int)r.c0;
+        const size_t n = (size_t)r.n;
+        if ((rc = put(m_.inc_off + r.c0, L.inc_off.data(), 4 * (n + 1)))) return rc;
+        if ((rc = put(m_.inc + r.i0, L.inc.data(), 4 * (size_t)r.k))) return rc;
+        if ((rc = put(m_.nbr + r.i0, L.nbr.data(), 4 * (size_t)r.k))) return rc;
+        if ((rc = put(m_.fc1 + r.f0, L.fc1.data(), 4 * (size_t)r.m))) return rc;
+        if ((rc = put(m_.fc2 + r.f0, L.fc2.data(), 4 * (size_t)r.m))) return rc;
+        if ((rc = put(m_.qcell + r.f0, L.qcell.data(), 4 * (size_t)r.m))) return rc;
+        if ((rc = put(m_.Ixx + r.c0, L.Ixx.data(), 8 * n))) return rc;
+        if ((rc = put(m_.Iyy + r.c0, L.Iyy.data(), 8 * n))) return rc;
+        if ((rc = put(m_.Ixy + r.c0, L.Ixy.data(), 8 * n))) return rc;
+        if ((rc = putT((T*)m_.vol + r.c0, L.vol))) return rc;
+        for (int gI = 0; gI < 14; gI++) if ((rc = putT(geo_[gI] + r.f0, L.fgeo[gI]))) return rc;
+        // parameters and the uniform freestream state (main.cpp:75-118)
+        SolveParams<T> p{};
+        const double gm1 = cs->gamma - 1, Cp = cs->R * cs->gamma / (cs->gamma - 1), kc = (cs->mu * Cp) / cs->Pr;
+        const double E = (cs->P / (cs->gamma - 1)) + 0.5 * cs->rho * (cs->u * cs->u + cs->v * cs->v);
+        p.k.gamma = (T)cs->gamma; p.k.gm1 = (T)gm1; p.k.R = (T)cs->R; p.k.mu = (T)cs->mu; p.k.k = (T)kc;
+        p.k.q_inf[0] = (T)cs->rho; p.k.q_inf[1] = (T)(cs->rho * cs->u); p.k.q_inf[2] = (T)(cs->rho * cs->v); p.k.q_inf[3] = (T)E;
+        p.k.rho_inf = (T)cs->rho; p.k.u_inf = (T)cs->u; p.k.v_inf = (T)cs->v; p.k.P_inf = (T)cs->P;
+        p.k.two_cfl = (T)(2 * cs->cfl);
+        p.k.vn0 = (T)std::sqrt(cs->v * cs->v + cs->u * cs->u);
+        p.k.c0 = (T)std::sqrt(cs->gamma * (cs->P / cs->rho));
+        p.order2 = cs->order == 2; p.ns = cs->eqn == FV2D_NS; p.squeeze = cs->limiter == FV2D_LIM_SQUEEZE;
+        p.global_dt = cs->time_type == FV2D_DT_GLOBAL; p.fresh = 1; p.init_prims = 1;
+        if ((rc = put(P_ + sid, &p, sizeof(p)))) return rc;
+        // as the single-solve upload: hi = the state rounded to T, lo = the rounded remainder
+        const double qd[4] = {cs->rho, cs->rho * cs->u, cs->rho * cs->v, E};
+        Q4<T> hi1, lo1;
+        for (int j = 0; j < 4; j++) { hi1.p[j] = (T)qd[j]; lo1.p[j] = (T)(qd[j] - (double)hi1.p[j]); }
+        std::vector<Q4<T>> q(n, hi1);
+        if ((rc = put(Q_[0] + r.c0, q.data(), sizeof(Q4<T>) * n))) return rc;
+        if (Qlo_) {
+            std::fill(q.begin(), q.end(), lo1);
+            if ((rc = put(Qlo_ + r.c0, q.data(), sizeof(Q4<T>) * n))) return rc;
+        }
+        int zero = 0;
+        if ((rc = put(flags_ + sid, &zero, 4))) return rc;
+        FV2D_B(cudaMemsetAsync(smax_ + sid, 0, sizeof(T), stream_));
+        k_spectral_init<T><<<(int)((n + 255) / 256), 256, 0, stream_>>>((int)n, m_.inc_off + r.c0, m_.inc, m_.g.area,
+                                                                         S_arr_ + r.c0, smax_ + sid, p.k);
+        FV2D_B(cudaGetLastError());
+        r.n2o = hm.cell_new2old;
+        r.active = true;
+        recs_[sid] = std::move(r);
+        *sid_out = sid;
+        return rebuild_tiles();
+    }
+
+    int remove(int sid) override {
+        if (sid < 0 || sid >= S_ || !recs_[sid].active) { err_ = "no such solve"; return FV2D_ERR_ARG; }
+        FV2D_B(cudaStreamSynchronize(stream_));
+        Rec& r = recs_[sid];
+        cells_.release(r.c0, r.n + 1);
+        faces_.release(r.f0, r.m);
+        incs_.release(r.i0, r.k);
+        r = Rec();
+        return rebuild_tiles();
+    }
+
+    int step(int iterations) override {
+        if (iterations < 0) { err_ = "negative iteration count"; return FV2D_ERR_ARG; }
+        if (n_ctiles_ == 0) return FV2D_OK;
+        for (int it = 0; it < iterations; it++) {
+            if (timing_) {
+                int rc = launch_iteration();
+                if (rc) return rc;
+            } else {
+                if (!graph_) {
+                    cudaGraph_t g;
+                    FV2D_B(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+                    int rc = launch_iteration();
+                    cudaError_t e = cudaStreamEndCapture(stream_, &g);
+                    if (rc) return rc;
+                    if (e != cudaSuccess) { err_ = std::string("graph capture: ") + cudaGetErrorString(e); return FV2D_ERR_CUDA; }
+                    e = cudaGraphInstantiate(&graph_, g, 0);
+                    cudaGraphDestroy(g);
+                    if (e != cudaSuccess) { graph_ = nullptr; err_ = std::string("graph instantiate: ") + cudaGetErrorString(e); return FV2D_ERR_CUDA; }
+                }
+                FV2D_B(cudaGraphLaunch(graph_, stream_));
+            }
+            for (auto& r : recs_) if (r.active) r.iterations++;
+        }
+        return FV2D_OK;
+    }
+
+    int norms(int* sids, double* out, int* iters, int max, int* n) override {
+        int rc = synchronize();
+        std::vector<double> h(4 * (size_t)S_);
+        FV2D_B(cudaMemcpy(h.data(), res2_, 32 * (size_t)S_, cudaMemcpyDeviceToHost));
+        int k = 0;
+        for (int s = 0; s < S_ && k < max; s++) {
+            if (!recs_[s].active) continue;
+            sids[k] = s;
+            if (iters) iters[k] = recs_[s].iterations;
+            for (int j = 0; j < 4; j++) out[4 * k + j] = std::sqrt(h[4 * s + j]);
+            k++;
+        }
+        *n = k;
+        return rc;
+    }
+
+    int get_state(int sid, double* q) override {
+        if (sid < 0 || sid >= S_ || !recs_[sid].active) { err_ = "no such solve"; return FV2D_ERR_ARG; }
+        const Rec& r = recs_[sid];
+        std::vector<Q4<T>> h(r.n), lo(Qlo_ ? r.n : 0);
+        FV2D_B(cudaStreamSynchronize(stream_));
+        FV2D_B(cudaMemcpy(h.data(), Q_[0] + r.c0, sizeof(Q4<T>) * r.n, cudaMemcpyDeviceToHost));
+        if (Qlo_) FV2D_B(cudaMemcpy(lo.data(), Qlo_ + r.c0, sizeof(Q4<T>) * r.n, cudaMemcpyDeviceToHost));
+        for (long long c = 0; c < r.n; c++) {
+            const int o = r.n2o[c];
+            for (int j = 0; j < 4; j++) q[(size_t)j * r.n + o] = (double)h[c].p[j] + (Qlo_ ? (double)lo[c].p[j] : 0.0);
+        }
+        int f = 0;
+        FV2D_B(cudaMemcpy(&f, flags_ + sid, 4, cudaMemcpyDeviceToHost));
+        if (f) { err_ = "non-physical state (rho <= 0, E <= 0 or NaN) in this solve"; return FV2D_ERR_STATE; }
+        return FV2D_OK;
+    }
+
+    int synchronize() override {
+        FV2D_B(cudaStreamSynchronize(stream_));
+        return FV2D_OK;
+    }
+
+    int set_tuning(const BatchTuning& t) override {
+        if (t.block < 64 || t.block > 512 || (t.block & 31)) { err_ = "block must be a multiple of 32 in [64, 512]"; return FV2D_ERR_ARG; }
+        for (int b = 0; b < 3; b++) if (t.tile_mult[b] < 1 || t.tile_mult[b] > 64) { err_ = "tile multiple out of range"; return FV2D_ERR_ARG; }
+        FV2D_B(cudaStreamSynchronize(stream_));
+        tune_ = t;
+        compute_grids();
+        if (graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
+        return rebuild_tiles();
+    }
+    BatchTuning tuning() const override { return tune_; }
+
+    int usage(long long* o) override {
+        long long act = 0;
+        for (auto& r : recs_) act += r.active;
+        o[0] = cells_.used(); o[1] = cells_.cap(); o[2] = faces_.used(); o[3] = faces_.cap();
+        o[4] = incs_.used(); o[5] = incs_.cap(); o[6] = act; o[7] = (long long)bytes_;
+        return FV2D_OK;
+    }
+
+    int set_timing(int enable) override {
+        timing_ = enable != 0;
+        for (int i = 0; i < 3; i++) { ms_[i] = 0; launches_[i] = 0; }
+        return FV2D_OK;
+    }
+    int kernel_times(double* ms, int* launches) override {
+        FV2D_B(cudaStreamSynchronize(stream_));
+        for (auto& p : pending_) {
+            float t = 0;
+            cudaEventElapsedTime(&t, p.a, p.b);
+            ms_[p.kid] += t; launches_[p.kid] += 1;
+            free_events_.push_back(p.a); free_events_.push_back(p.b);
+        }
+        pending_.clear();
+        for (int i = 0; i < 3; i++) { ms[i] = ms_[i]; launches[i] = launches_[i]; }
+        return FV2D_OK;
+    }
+    void* stream() override { return (void*)stream_; }
+
+private:
+    int put(const void* dst_c, const void* src, size_t bytes) {
+        void* dst = const_cast<void*>(dst_c);
+        if (bytes == 0) return FV2D_OK;
+        if (bytes > pin_bytes_) {
+            if (pin_) cudaFreeHost(pin_);
+            pin_ = nullptr;
+            pin_bytes_ = 0;
+            FV2D_B(cudaMallocHost(&pin_, bytes));
+            pin_bytes_ = bytes;
+        }
+        FV2D_B(cudaStreamSynchronize(stream_));
+        std::memcpy(pin_, src, bytes);
+        FV2D_B(cudaMemcpyAsync(dst, pin_, bytes, cudaMemcpyHostToDevice, stream_));
+        FV2D_B(cudaStreamSynchronize(stream_));
+        return FV2D_OK;
+    }
+    int putT(T* dst, const std::vector<double>& src) {
+        std::vector<T> h(src.size());
+        for (size_t i = 0; i < src.size(); i++) h[i] = (T)src[i];
+        return put(dst, h.data(), sizeof(T) * h.size());
+    }
+
+    int bucket(long long cells) const {
+        return cells < tune_.bucket_edges[0] ? 0 : cells < tune_.bucket_edges[1] ? 1 : 2;
+    }
+
+    int rebuild_tiles() {
+        std::vector<Tile> tc, tf;
+        for (int s = 0; s < S_; s++) {
+            const Rec& r = recs_[s];
+            if (!r.active) continue;
+            const long long tile = (long long)tune_.block * tune_.tile_mult[bucket(r.n)];
+            for (long long c = 0; c < r.n; c += tile) tc.push_back(Tile{s, (int)(r.c0 + c), (int)std::min(tile, r.n - c), 0});
+            for (long long f = 0; f < r.m; f += tile) tf.push_back(Tile{s, (int)(r.f0 + f), (int)std::min(tile, r.m - f), 0});
+        }
+        if ((int)tc.size() > tile_cap_ || (int)tf.size() > tile_cap_) { err_ = "tile list capacity exceeded"; return FV2D_ERR_NOMEM; }
+        int rc;
+        if (!tc.empty() && (rc = put(tc_, tc.data(), sizeof(Tile) * tc.size()))) return rc;
+        if (!tf.empty() && (rc = put(tf_, tf.data(), sizeof(Tile) * tf.size()))) return rc;
+        int cnt[2] = {(int)tc.size(), (int)tf.size()};
+        if ((rc = put(cnt_, cnt, sizeof(cnt)))) return rc;
+        n_ctiles_ = cnt[0];
+        n_ftiles_ = cnt[1];
+        return FV2D_OK;
+    }
+
+    template <class F>
+    void timed(int kid, F&& fn) {
+        if (!timing_) { fn(); return; }
+        Pending p{kid, ev(), ev()};
+        cudaEventRecord(p.a, stream_);
+        fn();
+        cudaEventRecord(p.b, stream_);
+        pending_.push_back(p);
+    }
+    cudaEvent_t ev() {
+        if (!free_events_.empty()) { cudaEvent_t e = free_events_.back(); free_events_.pop_back(); return e; }
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        return e;
+    }
+
+    int grid_for(const void* kernel) {
+        int per = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, tune_.block, 0);
+        return std::max(1, per) * sms_;
+    }
+    void compute_grids() {
+        gg_ = grid_for((const void*)kb_gradient<T>);
+        gf_[0] = grid_for((const void*)kb_face<T, false>);
+        gf_[1] = grid_for((const void*)kb_face<T, true>);
+        gu_[0] = grid_for((const void*)kb_update<T, 0>);
+        gu_[1] = grid_for((const void*)kb_update<T, 1>);
+        gu_[2] = grid_for((const void*)kb_update<T, 2>);
+    }
+
+    int launch_iteration() {
+        const int B = tune_.block;
+        const int* nct = cnt_;
+        const int* nft = cnt_ + 1;
+        for (int s = 0; s < 3; s++) {
+            const int p = (s + 2) % 3;
+            timed(0, [&] {
+                kb_gradient<T><<<gg_, B, 0, stream_>>>(tc_, nct, m_, P_, Q_[s], Q_[p], G_[p], G_[s]);
+            });
+            timed(1, [&] {
+                if (s == 2)
+                    kb_face<T, true><<<gf_[1], B, 0, stream_>>>(tf_, nft, m_, P_, Q_[s], G_[s], t_, s_);
+                else
+                    kb_face<T, false><<<gf_[0], B, 0, stream_>>>(tf_, nft, m_, P_, Q_[s], G_[s], t_, s_);
+            });
+            if (s == 2) {
+                FV2D_B(cudaMemsetAsync(smax_, 0, sizeof(T) * S_, stream_));
+                FV2D_B(cudaMemsetAsync(res2_, 0, 32 * (size_t)S_, stream_));
+            }
+            timed(2, [&] {
+                if (s == 0)
+                    kb_update<T, 0><<<gu_[0], B, 0, stream_>>>(tc_, nct, m_, P_, t_, s_, Q_[0], Q_[1], Q_[2], dt_, S_arr_, smax_, res2_, flags_, D_, Qlo_);
+                else if (s == 1)
+                    kb_update<T, 1><<<gu_[1], B, 0, stream_>>>(tc_, nct, m_, P_, t_, s_, Q_[0], Q_[1], Q_[2], dt_, S_arr_, smax_, res2_, flags_, D_, Qlo_);
+                else
+                    kb_update<T, 2><<<gu_[2], B, 0, stream_>>>(tc_, nct, m_, P_, t_, s_, Q_[0], Q_[1], Q_[2], dt_, S_arr_, smax_, res2_, flags_, D_, Qlo_);
+            });
+            FV2D_B(cudaGetLastError());
+        }
+        return FV2D_OK;
+    }
+    struct Pending { int kid; cudaEvent_t a, b; };
+
+    long long Nc_ = 0, Fc_ = 0, Ic_ = 0;
+    int S_ = 0, sms_ = 1, tile_cap_ = 0, n_ctiles_ = 0, n_ftiles_ = 0;
+    int gg_ = 1, gf_[2] = {1, 1}, gu_[3] = {1, 1, 1};
+    BatchTuning tune_;
+    cudaStream_t stream_ = nullptr;
+    cudaGraphExec_t graph_ = nullptr;
+    void* arena_ = nullptr;
+    size_t bytes_ = 0;
+    void* pin_ = nullptr;
+    size_t pin_bytes_ = 0;
+    Q4<T>* Q_[3] = {nullptr, nullptr, nullptr};
+    Q4<T>* G_[3] = {nullptr, nullptr, nullptr};
+    T *dt_ = nullptr, *S_arr_ = nullptr, *s_ = nullptr, *smax_ = nullptr;
+    T* geo_[14] = {nullptr};
+    Q4<T>* t_ = nullptr;
+    Q4<T>* D_ = nullptr;     // FP32 only: RK increment in delta form
+    Q4<T>* Qlo_ = nullptr;   // FP32 only: compensation term of Qn
+    SolveParams<T>* P_ = nullptr;
+    double* res2_ = nullptr;
+    int* flags_ = nullptr;
+    Tile *tc_ = nullptr, *tf_ = nullptr;
+    int* cnt_ = nullptr;
+    DevMesh<T> m_{};
+    RangeAlloc cells_, faces_, incs_;
+    std::vector<Rec> recs_;
+    bool timing_ = false;
+    std::vector<Pending> pending_;
+    std::vector<cudaEvent_t> free_events_;
+    double ms_[3] = {0, 0, 0};
+    int launches_[3] = {0, 0, 0};
+};
+
+#undef FV2D_B
+
+}  // namespace fv2d

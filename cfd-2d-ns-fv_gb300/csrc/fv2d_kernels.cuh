@@ -37,6 +37,15 @@ struct FaceGeo {
     const T *nx, *ny, *area, *c1dx, *c1dy, *c2dx, *c2dy, *dxj, *dyj, *mx, *my, *lx, *ly, *dist;
 };
 
+// Every mesh array a stage reads, device order (single solve) or arena order (batch).
+template <class T>
+struct DevMesh {
+    const int *inc_off, *inc, *nbr, *fc1, *fc2, *qcell;
+    FaceGeo<T> g;
+    const double *Ixx, *Iyy, *Ixy;
+    const T* vol;
+};
+
 template <class T>
 __device__ __forceinline__ Q4<T> ldq(const Q4<T>* __restrict__ a, int i) {
     return a[i];
@@ -76,14 +85,15 @@ __device__ __forceinline__ void cons(T rho, T u, T v, T P, const Consts<T>& k, T
 // gradient with the reconstruction's own expression, or are the -101 sentinel the face states
 // start with (class_q.hpp:73-76) on the first stage after initialisation.
 template <class T, bool SQUEEZE>
-__global__ void __launch_bounds__(256)
-k_gradient(int nc, const int* __restrict__ inc_off, const int* __restrict__ inc, const int* __restrict__ nbr,
-           const int* __restrict__ qcell, FaceGeo<T> g, const double* __restrict__ Ixx,
-           const double* __restrict__ Iyy, const double* __restrict__ Ixy, const Q4<T>* __restrict__ Q,
-           const Q4<T>* __restrict__ Qprev, const Q4<T>* __restrict__ Gprev, Q4<T>* __restrict__ Gout,
-           Consts<T> k, int first_stage, int init_prims) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= nc) return;
+__device__ __forceinline__ void gradient_cell(int c, const DevMesh<T>& m, const Q4<T>* __restrict__ Q,
+                                              const Q4<T>* __restrict__ Qprev, const Q4<T>* __restrict__ Gprev,
+                                              Q4<T>* __restrict__ Gout, const Consts<T>& k, int first_stage,
+                                              int init_prims) {
+    const int* __restrict__ inc_off = m.inc_off;
+    const int* __restrict__ inc = m.inc;
+    const int* __restrict__ nbr = m.nbr;
+    const int* __restrict__ qcell = m.qcell;
+    const FaceGeo<T>& g = m.g;
     const Q4<T> qc = ldq(Q, c);
     T sx[4] = {T(0), T(0), T(0), T(0)}, sy[4] = {T(0), T(0), T(0), T(0)};
     T qmin[4], qmax[4];
@@ -136,7 +146,7 @@ k_gradient(int nc, const int* __restrict__ inc_off, const int* __restrict__ inc,
 #pragma unroll
         for (int j = 0; j < 4; j++) { sx[j] += d[j] * fx; sy[j] += d[j] * fy; }
     }
-    const T ixx = (T)Ixx[c], iyy = (T)Iyy[c], ixy = (T)Ixy[c];
+    const T ixx = (T)m.Ixx[c], iyy = (T)m.Iyy[c], ixy = (T)m.Ixy[c];
     Q4<T> gx, gy;
 #pragma unroll
     for (int j = 0; j < 4; j++) {
@@ -167,6 +177,15 @@ k_gradient(int nc, const int* __restrict__ inc_off, const int* __restrict__ inc,
     Gout[2 * c + 1] = gy;
 }
 
+template <class T, bool SQUEEZE>
+__global__ void __launch_bounds__(256)
+k_gradient(int nc, DevMesh<T> m, const Q4<T>* __restrict__ Q, const Q4<T>* __restrict__ Qprev,
+           const Q4<T>* __restrict__ Gprev, Q4<T>* __restrict__ Gout, Consts<T> k, int first_stage, int init_prims) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    gradient_cell<T, SQUEEZE>(c, m, Q, Qprev, Gprev, Gout, k, first_stage, init_prims);
+}
+
 // ------------------------------------------------------------------------------------------
 // Face kernel: reconstruction + boundary ghosts (reconstruction.cpp:22-80), NS face terms
 // (reconstruction.cpp:86-164, class_q.hpp:163-169, class_f.hpp:52-59), Rusanov flux
@@ -174,13 +193,11 @@ k_gradient(int nc, const int* __restrict__ inc_off, const int* __restrict__ inc,
 // Writes t = (V*A) - (F*A) per face and, on the last stage of an iteration, the spectral term
 // (|Vn_avg| + c_avg)*A that the next time step sums (ssp_rk3.cpp:28-36).
 template <class T, bool ORDER2, bool NS, bool LAST>
-__global__ void __launch_bounds__(256)
-k_face(int nf, const int* __restrict__ fc1, const int* __restrict__ fc2, FaceGeo<T> g,
-       const Q4<T>* __restrict__ Q, const Q4<T>* __restrict__ G, Q4<T>* __restrict__ tout,
-       T* __restrict__ sout, Consts<T> k, int init_prims) {
-    const int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= nf) return;
-    const int c1 = fc1[f], c2 = fc2[f];
+__device__ __forceinline__ void face_flux(int f, const DevMesh<T>& m, const Q4<T>* __restrict__ Q,
+                                          const Q4<T>* __restrict__ G, Q4<T>* __restrict__ tout,
+                                          T* __restrict__ sout, const Consts<T>& k, int init_prims) {
+    const FaceGeo<T>& g = m.g;
+    const int c1 = m.fc1[f], c2 = m.fc2[f];
     const T fnx = g.nx[f], fny = g.ny[f], A = g.area[f];
     const Q4<T> q1 = ldq(Q, c1);
     Q4<T> g1x, g1y;
@@ -300,6 +317,15 @@ k_face(int nf, const int* __restrict__ fc1, const int* __restrict__ fc2, FaceGeo
     if (LAST) sout[f] = (fabs(vna) + ca) * A;
 }
 
+template <class T, bool ORDER2, bool NS, bool LAST>
+__global__ void __launch_bounds__(256)
+k_face(int nf, DevMesh<T> m, const Q4<T>* __restrict__ Q, const Q4<T>* __restrict__ G, Q4<T>* __restrict__ tout,
+       T* __restrict__ sout, Consts<T> k, int init_prims) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nf) return;
+    face_flux<T, ORDER2, NS, LAST>(f, m, Q, G, tout, sout, k, init_prims);
+}
+
 // ------------------------------------------------------------------------------------------
 // Spectral sums S_c = sum_f (|Vn_avg| + c_avg) A_f in ascending original face id
 // (ssp_rk3.cpp:28-36).  s == nullptr: the initial Vn_avg, c_avg of every face (class_q.hpp:61-62).
@@ -350,90 +376,162 @@ k_spectral_init(int nc, const int* __restrict__ inc_off, const int* __restrict__
 // STAGE 1: Q2 = 0.75*Qn + 0.25*Q1 + 0.25*dt*R
 // STAGE 2: Qn = 1/3*Qn + 2/3*Q2 + 2/3*dt*R, and the spectral sums for the next iteration.
 // Non-physical results (rho <= 0, E <= 0, NaN) raise bit 0 of *flag; values are kept as computed.
+// FP32 keeps the RK increments in delta form and the base state as a compensated pair
+// (hi + lo, error-free TwoSum), so increments below half an ulp of the state are not lost:
+//   D1 = dt R1,               Q1 = hi + D1
+//   D2 = D1/4 + dt R2 / 4,    Q2 = hi + D2
+//   (hi, lo) += 2/3 D2 + 2/3 dt R3
+// which is the SSP-RK3 combination of ssp_rk3.cpp:50-77 rewritten about Qn.  Gradients and fluxes
+// read the FP32 stage states (hi, Q1, Q2).  FP64 (D == nullptr) keeps the reference's expressions.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bp = s - a;
+    e = (a - (s - bp)) + (b - bp);
+}
+
+template <class T, int STAGE>
+__device__ __forceinline__ T update_cell(int c, const DevMesh<T>& m, const Q4<T>* __restrict__ tface,
+                                         const T* __restrict__ sface, Q4<T>* __restrict__ Qn, Q4<T>* __restrict__ Q1,
+                                         Q4<T>* __restrict__ Q2, T* __restrict__ dt, T* __restrict__ S, T smax,
+                                         Q4<T>* __restrict__ Rout, int* __restrict__ flag, const Consts<T>& k,
+                                         int global_dt, T r[4], Q4<T>* __restrict__ D, Q4<T>* __restrict__ Qlo) {
+    const int* __restrict__ inc = m.inc;
+    T snext = T(0);
+#pragma unroll
+    for (int j = 0; j < 4; j++) r[j] = T(0);
+    const int b = m.inc_off[c], e = m.inc_off[c + 1];
+    for (int i = b; i < e; i++) {
+        const int f = inc[i] >> 1;
+        const Q4<T> t = ldq(tface, f);
+        if (inc[i] & 1) {
+#pragma unroll
+            for (int j = 0; j < 4; j++) r[j] -= t.p[j];
+        } else {
+#pragma unroll
+            for (int j = 0; j < 4; j++) r[j] += t.p[j];
+        }
+    }
+    const T vc = m.vol[c];
+#pragma unroll
+    for (int j = 0; j < 4; j++) r[j] = r[j] / vc;
+    if (Rout) { Q4<T> rr; for (int j = 0; j < 4; j++) rr.p[j] = r[j]; Rout[c] = rr; }
+    const Q4<T> qn = ldq(Qn, c);
+    Q4<T> out;
+    T dtc;
+    if (STAGE == 0) {
+        dtc = (k.two_cfl * vc) / (global_dt ? smax : S[c]);
+        dt[c] = dtc;
+    } else {
+        dtc = dt[c];
+    }
+    if constexpr (sizeof(T) == 4) {
+        if (D) {
+            Q4<T> d;
+            if (STAGE == 0) {
+#pragma unroll
+                for (int j = 0; j < 4; j++) { d.p[j] = dtc * r[j]; out.p[j] = qn.p[j] + d.p[j]; }
+                D[c] = d;
+                Q1[c] = out;
+            } else if (STAGE == 1) {
+                const Q4<T> d1 = ldq((const Q4<T>*)D, c);
+#pragma unroll
+                for (int j = 0; j < 4; j++) { d.p[j] = T(0.25) * d1.p[j] + T(0.25) * dtc * r[j]; out.p[j] = qn.p[j] + d.p[j]; }
+                D[c] = d;
+                Q2[c] = out;
+            } else {
+                const Q4<T> d2 = ldq((const Q4<T>*)D, c);
+                Q4<T> lo = ldq((const Q4<T>*)Qlo, c);
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const T inc_j = T(2.0 / 3.0) * d2.p[j] + T(2.0 / 3.0) * dtc * r[j];
+                    T s, err;
+                    two_sum(qn.p[j], lo.p[j] + inc_j, s, err);
+                    out.p[j] = s;
+                    lo.p[j] = err;
+                }
+                Qn[c] = out;
+                Qlo[c] = lo;
+                for (int i = b; i < e; i++) snext += sface[inc[i] >> 1];
+                S[c] = snext;
+            }
+            if (!(out.p[0] > T(0)) || !(out.p[3] > T(0))) atomicOr(flag, 1);
+            return snext;
+        }
+    }
+    if (STAGE == 0) {
+#pragma unroll
+        for (int j = 0; j < 4; j++) out.p[j] = qn.p[j] + dtc * r[j];
+        Q1[c] = out;
+    } else if (STAGE == 1) {
+        const Q4<T> q1 = ldq(Q1, c);
+#pragma unroll
+        for (int j = 0; j < 4; j++) out.p[j] = T(0.75) * qn.p[j] + T(0.25) * q1.p[j] + T(0.25) * dtc * r[j];
+        Q2[c] = out;
+    } else {
+        const Q4<T> q2 = ldq(Q2, c);
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+            out.p[j] = T(1.0 / 3.0) * qn.p[j] + T(2.0 / 3.0) * q2.p[j] + T(2.0 / 3.0) * dtc * r[j];
+        Qn[c] = out;
+        for (int i = b; i < e; i++) snext += sface[inc[i] >> 1];
+        S[c] = snext;
+    }
+    if (!(out.p[0] > T(0)) || !(out.p[3] > T(0))) atomicOr(flag, 1);
+    return snext;
+}
+
 template <class T, int STAGE>
 __global__ void __launch_bounds__(256)
-k_update(int nc, const int* __restrict__ inc_off, const int* __restrict__ inc, const Q4<T>* __restrict__ tface,
-         const T* __restrict__ sface, const T* __restrict__ vol, Q4<T>* __restrict__ Qn, Q4<T>* __restrict__ Q1,
-         Q4<T>* __restrict__ Q2, T* __restrict__ dt, T* __restrict__ S, T* __restrict__ smax, Q4<T>* __restrict__ Rout,
-         int* __restrict__ flag, Consts<T> k, int global_dt) {
+k_update(int nc, DevMesh<T> m, const Q4<T>* __restrict__ tface, const T* __restrict__ sface, Q4<T>* __restrict__ Qn,
+         Q4<T>* __restrict__ Q1, Q4<T>* __restrict__ Q2, T* __restrict__ dt, T* __restrict__ S, T* __restrict__ smax,
+         Q4<T>* __restrict__ Rout, int* __restrict__ flag, Consts<T> k, int global_dt, Q4<T>* __restrict__ D,
+         Q4<T>* __restrict__ Qlo) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     T snext = T(0);
     if (c < nc) {
-        T r[4] = {T(0), T(0), T(0), T(0)};
-        const int b = inc_off[c], e = inc_off[c + 1];
-        for (int i = b; i < e; i++) {
-            const int f = inc[i] >> 1;
-            const Q4<T> t = ldq(tface, f);
-            if (inc[i] & 1) {
-#pragma unroll
-                for (int j = 0; j < 4; j++) r[j] -= t.p[j];
-            } else {
-#pragma unroll
-                for (int j = 0; j < 4; j++) r[j] += t.p[j];
-            }
-        }
-        const T vc = vol[c];
-#pragma unroll
-        for (int j = 0; j < 4; j++) r[j] = r[j] / vc;
-        if (Rout) { Q4<T> rr; for (int j = 0; j < 4; j++) rr.p[j] = r[j]; Rout[c] = rr; }
-        const Q4<T> qn = ldq(Qn, c);
-        Q4<T> out;
-        T dtc;
-        if (STAGE == 0) {
-            dtc = (k.two_cfl * vc) / (global_dt ? *smax : S[c]);
-            dt[c] = dtc;
-#pragma unroll
-            for (int j = 0; j < 4; j++) out.p[j] = qn.p[j] + dtc * r[j];
-            Q1[c] = out;
-        } else if (STAGE == 1) {
-            dtc = dt[c];
-            const Q4<T> q1 = ldq(Q1, c);
-#pragma unroll
-            for (int j = 0; j < 4; j++) out.p[j] = T(0.75) * qn.p[j] + T(0.25) * q1.p[j] + T(0.25) * dtc * r[j];
-            Q2[c] = out;
-        } else {
-            dtc = dt[c];
-            const Q4<T> q2 = ldq(Q2, c);
-#pragma unroll
-            for (int j = 0; j < 4; j++)
-                out.p[j] = T(1.0 / 3.0) * qn.p[j] + T(2.0 / 3.0) * q2.p[j] + T(2.0 / 3.0) * dtc * r[j];
-            Qn[c] = out;
-            for (int i = b; i < e; i++) snext += sface[inc[i] >> 1];
-            S[c] = snext;
-        }
-        if (!(out.p[0] > T(0)) || !(out.p[3] > T(0))) atomicOr(flag, 1);
+        T r[4];
+        snext = update_cell<T, STAGE>(c, m, tface, sface, Qn, Q1, Q2, dt, S, (STAGE == 0 && global_dt) ? *smax : T(0),
+                                      Rout, flag, k, global_dt, r, D, Qlo);
     }
     if (STAGE == 2) {
-        const T m = block_max(c < nc ? snext : T(0));
-        if (threadIdx.x == 0) atomic_max_pos(smax, m);
+        const T mx = block_max(c < nc ? snext : T(0));
+        if (threadIdx.x == 0) atomic_max_pos(smax, mx);
     }
 }
 
 // ------------------------------------------------------------------------------------------
 // Host-format <-> device-format state (SoA double in file numbering <-> AoS T in device order).
 template <class T>
-__global__ void k_state_in(int nc, const int* __restrict__ new2old, const double* __restrict__ q, Q4<T>* __restrict__ Q) {
+__global__ void k_state_in(int nc, const int* __restrict__ new2old, const double* __restrict__ q, Q4<T>* __restrict__ Q,
+                           Q4<T>* __restrict__ Qlo) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= nc) return;
     const int o = new2old[c];
-    Q4<T> v;
+    Q4<T> v, lo;
 #pragma unroll
-    for (int j = 0; j < 4; j++) v.p[j] = (T)q[(size_t)j * nc + o];
+    for (int j = 0; j < 4; j++) {
+        const double x = q[(size_t)j * nc + o];
+        v.p[j] = (T)x;
+        lo.p[j] = (T)(x - (double)v.p[j]);
+    }
     Q[c] = v;
+    if (Qlo) Qlo[c] = lo;
 }
 
 template <class T>
 __global__ void k_state_out(int nc, int ncomp, const int* __restrict__ new2old, const Q4<T>* __restrict__ Q,
-                            double* __restrict__ q) {
-    // ncomp = 4 (state) or 8 (gradient pairs: x block then y block)
+                            double* __restrict__ q, const Q4<T>* __restrict__ Qlo) {
+    // ncomp = 4 (state; plus its compensation term when Qlo is given) or 8 (gradient pairs)
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= nc) return;
     const int o = new2old[c];
     const int per = ncomp / 4;
     for (int h = 0; h < per; h++) {
         const Q4<T> v = Q[(size_t)per * c + h];
+        Q4<T> lo;
+        if (Qlo) lo = Qlo[c];
 #pragma unroll
-        for (int j = 0; j < 4; j++) q[(size_t)(4 * h + j) * nc + o] = (double)v.p[j];
+        for (int j = 0; j < 4; j++) q[(size_t)(4 * h + j) * nc + o] = (double)v.p[j] + (Qlo ? (double)lo.p[j] : 0.0);
     }
 }
 

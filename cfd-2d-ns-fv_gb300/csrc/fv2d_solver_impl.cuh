@@ -76,6 +76,8 @@ public:
         size_t o_stage = take(8 * 8 * (size_t)nc_);
         nred_ = 304;
         size_t o_part = take(8 * 4 * (size_t)nred_);
+        const bool comp = sizeof(T) == 4;   // FP32: delta-form increments + compensated base state
+        size_t o_D = comp ? take(q4 * nc_) : 0, o_lo = comp ? take(q4 * nc_) : 0;
         arena_bytes_ = off;
         FV2D_CUDA(cudaMalloc(&arena_, arena_bytes_));
         char* a = (char*)arena_;
@@ -90,8 +92,12 @@ public:
         g_.c2dx = geo[5]; g_.c2dy = geo[6]; g_.dxj = geo[7]; g_.dyj = geo[8];
         g_.mx = geo[9]; g_.my = geo[10]; g_.lx = geo[11]; g_.ly = geo[12]; g_.dist = geo[13];
         t_ = (Q4<T>*)(a + o_t); s_ = (T*)(a + o_s);
+        dm_.inc_off = inc_off_; dm_.inc = inc_; dm_.nbr = nbr_; dm_.fc1 = fc1_; dm_.fc2 = fc2_; dm_.qcell = qcell_;
+        dm_.g = g_; dm_.Ixx = Ixx_; dm_.Iyy = Iyy_; dm_.Ixy = Ixy_; dm_.vol = vol_;
         smax_ = (T*)(a + o_smax); flag_ = (int*)(a + o_flag);
         n2o_ = (int*)(a + o_n2o); dstage_ = (double*)(a + o_stage); part_ = (double*)(a + o_part);
+        D_ = comp ? (Q4<T>*)(a + o_D) : nullptr;
+        Qlo_ = comp ? (Q4<T>*)(a + o_lo) : nullptr;
         FV2D_CUDA(cudaMemsetAsync(arena_, 0, arena_bytes_, stream_));
         // ---- upload (one pinned staging buffer reused for every array)
         staging_bytes_ = std::max<size_t>({sizeof(T) * (size_t)nf_, 8 * (size_t)nc_ * 8, 4 * (size_t)ninc_,
@@ -141,7 +147,7 @@ public:
     int upload_state(const double* q) {
         std::memcpy(host_stage_, q, 8 * 4 * (size_t)nc_);
         FV2D_CUDA(cudaMemcpyAsync(dstage_, host_stage_, 8 * 4 * (size_t)nc_, cudaMemcpyHostToDevice, stream_));
-        launch(K_STATE_IN, nc_, [&](int gr) { k_state_in<T><<<gr, 256, 0, stream_>>>(nc_, n2o_, dstage_, Q_[0]); });
+        launch(K_STATE_IN, nc_, [&](int gr) { k_state_in<T><<<gr, 256, 0, stream_>>>(nc_, n2o_, dstage_, Q_[0], Qlo_); });
         // fresh face histories: -101 sentinel for the limiter, initial Vn_avg/c_avg for dt
         FV2D_CUDA(cudaMemsetAsync(smax_, 0, 64, stream_));
         launch(K_SPECTRAL, nc_, [&](int gr) {
@@ -162,7 +168,7 @@ public:
         if (stage_ != 0) { err_ = "load_state between iterations only (stage counter is not 0)"; return FV2D_ERR_ARG; }
         std::memcpy(host_stage_, q, 8 * 4 * (size_t)nc_);
         FV2D_CUDA(cudaMemcpyAsync(dstage_, host_stage_, 8 * 4 * (size_t)nc_, cudaMemcpyHostToDevice, stream_));
-        launch(K_STATE_IN, nc_, [&](int gr) { k_state_in<T><<<gr, 256, 0, stream_>>>(nc_, n2o_, dstage_, Q_[0]); });
+        launch(K_STATE_IN, nc_, [&](int gr) { k_state_in<T><<<gr, 256, 0, stream_>>>(nc_, n2o_, dstage_, Q_[0], Qlo_); });
         FV2D_CUDA(cudaGetLastError());
         init_prims_ = false;
         return FV2D_OK;
@@ -175,11 +181,11 @@ public:
         if (order2_) {
             launch(K_GRADIENT, nc_, [&](int gr) {
                 if (squeeze_)
-                    k_gradient<T, true><<<gr, 256, 0, stream_>>>(nc_, inc_off_, inc_, nbr_, qcell_, g_, Ixx_, Iyy_, Ixy_,
-                                                                qin, Q_[p], G_[p], G_[s], k_, fresh_ ? 1 : 0, init_prims_ ? 1 : 0);
+                    k_gradient<T, true><<<gr, 256, 0, stream_>>>(nc_, dm_, qin, Q_[p], G_[p], G_[s], k_, fresh_ ? 1 : 0,
+                                                                init_prims_ ? 1 : 0);
                 else
-                    k_gradient<T, false><<<gr, 256, 0, stream_>>>(nc_, inc_off_, inc_, nbr_, qcell_, g_, Ixx_, Iyy_, Ixy_,
-                                                                 qin, Q_[p], G_[p], G_[s], k_, fresh_ ? 1 : 0, init_prims_ ? 1 : 0);
+                    k_gradient<T, false><<<gr, 256, 0, stream_>>>(nc_, dm_, qin, Q_[p], G_[p], G_[s], k_, fresh_ ? 1 : 0,
+                                                                 init_prims_ ? 1 : 0);
             });
         }
         launch(K_FACE, nf_, [&](int gr) { launch_face(gr, qin, G_[s], s == 2); });
@@ -187,11 +193,11 @@ public:
         Q4<T>* rout = (store_every_ || s == 2) ? R_ : nullptr;
         launch(K_UPDATE, nc_, [&](int gr) {
             if (s == 0)
-                k_update<T, 0><<<gr, 256, 0, stream_>>>(nc_, inc_off_, inc_, t_, s_, vol_, Q_[0], Q_[1], Q_[2], dt_, S_, smax_, rout, flag_, k_, global_dt_);
+                k_update<T, 0><<<gr, 256, 0, stream_>>>(nc_, dm_, t_, s_, Q_[0], Q_[1], Q_[2], dt_, S_, smax_, rout, flag_, k_, global_dt_, D_, Qlo_);
             else if (s == 1)
-                k_update<T, 1><<<gr, 256, 0, stream_>>>(nc_, inc_off_, inc_, t_, s_, vol_, Q_[0], Q_[1], Q_[2], dt_, S_, smax_, rout, flag_, k_, global_dt_);
+                k_update<T, 1><<<gr, 256, 0, stream_>>>(nc_, dm_, t_, s_, Q_[0], Q_[1], Q_[2], dt_, S_, smax_, rout, flag_, k_, global_dt_, D_, Qlo_);
             else
-                k_update<T, 2><<<gr, 256, 0, stream_>>>(nc_, inc_off_, inc_, t_, s_, vol_, Q_[0], Q_[1], Q_[2], dt_, S_, smax_, rout, flag_, k_, global_dt_);
+                k_update<T, 2><<<gr, 256, 0, stream_>>>(nc_, dm_, t_, s_, Q_[0], Q_[1], Q_[2], dt_, S_, smax_, rout, flag_, k_, global_dt_, D_, Qlo_);
         });
         FV2D_CUDA(cudaGetLastError());
         if (s == 0) { fresh_ = false; init_prims_ = false; }
@@ -268,7 +274,10 @@ public:
         if (ncomp == 1)
             launch(K_STATE_OUT, nc_, [&](int gr) { k_scalar_out<T><<<gr, 256, 0, stream_>>>(nc_, n2o_, (const T*)src, dstage_); });
         else
-            launch(K_STATE_OUT, nc_, [&](int gr) { k_state_out<T><<<gr, 256, 0, stream_>>>(nc_, ncomp, n2o_, (const Q4<T>*)src, dstage_); });
+            launch(K_STATE_OUT, nc_, [&](int gr) {
+                k_state_out<T><<<gr, 256, 0, stream_>>>(nc_, ncomp, n2o_, (const Q4<T>*)src, dstage_,
+                                                         field == FV2D_F_QBAR ? Qlo_ : nullptr);
+            });
         const size_t bytes = 8 * (size_t)ncomp * nc_;
         FV2D_CUDA(cudaMemcpyAsync(host_stage_, dstage_, bytes, cudaMemcpyDeviceToHost, stream_));
         FV2D_CUDA(cudaStreamSynchronize(stream_));
@@ -321,7 +330,7 @@ public:
 
 private:
     void launch_face(int gr, const Q4<T>* qin, const Q4<T>* G, bool last) {
-#define FV2D_FACE(O2, NS, LAST) k_face<T, O2, NS, LAST><<<gr, 256, 0, stream_>>>(nf_, fc1_, fc2_, g_, qin, G, t_, s_, k_, init_prims_ ? 1 : 0)
+#define FV2D_FACE(O2, NS, LAST) k_face<T, O2, NS, LAST><<<gr, 256, 0, stream_>>>(nf_, dm_, qin, G, t_, s_, k_, init_prims_ ? 1 : 0)
         if (order2_) {
             if (ns_) { if (last) FV2D_FACE(true, true, true); else FV2D_FACE(true, true, false); }
             else { if (last) FV2D_FACE(true, false, true); else FV2D_FACE(true, false, false); }
@@ -356,6 +365,7 @@ private:
     fv2d_case cs_{};
     Consts<T> k_{};
     FaceGeo<T> g_{};
+    DevMesh<T> dm_{};
     int nc_ = 0, nf_ = 0, ninc_ = 0, nred_ = 0;
     bool order2_ = false, ns_ = false, squeeze_ = false;
     int global_dt_ = 0;
@@ -371,6 +381,8 @@ private:
     Q4<T>* Q_[3] = {nullptr, nullptr, nullptr};
     Q4<T>* G_[3] = {nullptr, nullptr, nullptr};
     Q4<T>* R_ = nullptr;
+    Q4<T>* D_ = nullptr;     // FP32 only: RK increment in delta form
+    Q4<T>* Qlo_ = nullptr;   // FP32 only: compensation term of Qn
     Q4<T>* t_ = nullptr;
     T *dt_ = nullptr, *S_ = nullptr, *vol_ = nullptr, *s_ = nullptr, *smax_ = nullptr;
     double *Ixx_ = nullptr, *Iyy_ = nullptr, *Ixy_ = nullptr, *dstage_ = nullptr, *part_ = nullptr;

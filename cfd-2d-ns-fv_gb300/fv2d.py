@@ -29,6 +29,10 @@ EXPORTS = [
     "fv2d_step", "fv2d_stage", "fv2d_set_state", "fv2d_load_state", "fv2d_get_state", "fv2d_get_field", "fv2d_residual_norm",
     "fv2d_sizes", "fv2d_synchronize", "fv2d_set_store_residual", "fv2d_set_graphs", "fv2d_set_kernel_timing",
     "fv2d_kernel_times", "fv2d_stream", "fv2d_device_bytes", "fv2d_last_error", "fv2d_residual_noalloc",
+    "fv2d_batch_create", "fv2d_batch_destroy", "fv2d_batch_footprint", "fv2d_batch_add", "fv2d_batch_remove",
+    "fv2d_batch_step", "fv2d_batch_norms", "fv2d_batch_get_state", "fv2d_batch_synchronize", "fv2d_batch_set_tuning",
+    "fv2d_batch_get_tuning", "fv2d_batch_usage", "fv2d_batch_set_kernel_timing", "fv2d_batch_kernel_times",
+    "fv2d_batch_stream",
 ]
 
 
@@ -95,6 +99,21 @@ def library():
             "fv2d_stream": (vp, [vp]),
             "fv2d_device_bytes": (ctypes.c_longlong, [vp]),
             "fv2d_last_error": (ctypes.c_char_p, [vp]),
+            "fv2d_batch_create": (ctypes.c_int, [ctypes.c_longlong, ctypes.c_longlong, ctypes.c_int, ctypes.c_int, pvp]),
+            "fv2d_batch_destroy": (None, [vp]),
+            "fv2d_batch_footprint": (ctypes.c_int, [ctypes.POINTER(MeshDesc), ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)]),
+            "fv2d_batch_add": (ctypes.c_int, [vp, ctypes.POINTER(MeshDesc), ctypes.POINTER(Case), ip]),
+            "fv2d_batch_remove": (ctypes.c_int, [vp, ctypes.c_int]),
+            "fv2d_batch_step": (ctypes.c_int, [vp, ctypes.c_int]),
+            "fv2d_batch_norms": (ctypes.c_int, [vp, ip, dp, ip, ctypes.c_int, ip]),
+            "fv2d_batch_get_state": (ctypes.c_int, [vp, ctypes.c_int, dp]),
+            "fv2d_batch_synchronize": (ctypes.c_int, [vp]),
+            "fv2d_batch_set_tuning": (ctypes.c_int, [vp, ctypes.c_int, ip, ip]),
+            "fv2d_batch_get_tuning": (ctypes.c_int, [vp, ip, ip, ip]),
+            "fv2d_batch_usage": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_longlong)]),
+            "fv2d_batch_set_kernel_timing": (ctypes.c_int, [vp, ctypes.c_int]),
+            "fv2d_batch_kernel_times": (ctypes.c_int, [vp, dp, ip]),
+            "fv2d_batch_stream": (vp, [vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -284,3 +303,93 @@ class Solver:
 
     def device_bytes(self) -> int:
         return int(library().fv2d_device_bytes(self.h))
+
+
+class Batch:
+    """Many independent solves advanced together on one GPU (C ABI fv2d_batch_*)."""
+
+    def __init__(self, max_cells: int, max_faces: int, max_solves: int, precision: int = FP32):
+        lib = library()
+        h = ctypes.c_void_p()
+        _check(lib.fv2d_batch_create(max_cells, max_faces, max_solves, precision, ctypes.byref(h)))
+        self.h = h
+        self.precision = precision
+        self.cells = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            library().fv2d_batch_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    @staticmethod
+    def footprint(grid, precision: int = FP32) -> int:
+        d = _Desc(grid)
+        out = ctypes.c_longlong()
+        _check(library().fv2d_batch_footprint(ctypes.byref(d.desc), precision, ctypes.byref(out)))
+        return int(out.value)
+
+    def add(self, grid, case) -> int:
+        if isinstance(case, dict):
+            case = case_from_dict(case)
+        d = _Desc(grid)
+        sid = ctypes.c_int()
+        _check(library().fv2d_batch_add(self.h, ctypes.byref(d.desc), ctypes.byref(case), ctypes.byref(sid)))
+        self.cells[sid.value] = grid.num_cells
+        return sid.value
+
+    def remove(self, sid: int):
+        _check(library().fv2d_batch_remove(self.h, sid))
+        self.cells.pop(sid, None)
+
+    def step(self, iterations: int = 1):
+        _check(library().fv2d_batch_step(self.h, iterations))
+
+    def synchronize(self):
+        _check(library().fv2d_batch_synchronize(self.h))
+
+    def norms(self):
+        """{solve id: (norms[4], iterations)} for every active solve."""
+        mx = max(1, len(self.cells))
+        ids = np.zeros(mx, np.int32)
+        nr = np.zeros(4 * mx, np.float64)
+        it = np.zeros(mx, np.int32)
+        n = ctypes.c_int()
+        _check(library().fv2d_batch_norms(self.h, _ip(ids), _dp(nr), _ip(it), mx, ctypes.byref(n)))
+        return {int(ids[i]): (nr[4 * i:4 * i + 4].copy(), int(it[i])) for i in range(n.value)}
+
+    def get_state(self, sid: int):
+        out = np.empty(4 * self.cells[sid], np.float64)
+        _check(library().fv2d_batch_get_state(self.h, sid, _dp(out)))
+        return out
+
+    def set_tuning(self, block: int, tile_mult=(1, 2, 4), bucket_edges=(16384, 131072)):
+        tm = np.asarray(tile_mult, np.int32)
+        be = np.asarray(bucket_edges, np.int32)
+        _check(library().fv2d_batch_set_tuning(self.h, block, _ip(tm), _ip(be)))
+
+    def get_tuning(self):
+        b = ctypes.c_int()
+        tm = np.zeros(3, np.int32)
+        be = np.zeros(2, np.int32)
+        _check(library().fv2d_batch_get_tuning(self.h, ctypes.byref(b), _ip(tm), _ip(be)))
+        return int(b.value), tuple(int(x) for x in tm), tuple(int(x) for x in be)
+
+    def usage(self):
+        o = (ctypes.c_longlong * 8)()
+        _check(library().fv2d_batch_usage(self.h, o))
+        keys = ("cells_used", "cells_cap", "faces_used", "faces_cap", "incs_used", "incs_cap", "active", "bytes")
+        return dict(zip(keys, [int(v) for v in o]))
+
+    def set_kernel_timing(self, enable: bool):
+        _check(library().fv2d_batch_set_kernel_timing(self.h, int(enable)))
+
+    def kernel_times(self):
+        ms = np.zeros(3, np.float64)
+        ln = np.zeros(3, np.int32)
+        _check(library().fv2d_batch_kernel_times(self.h, _dp(ms), _ip(ln)))
+        return {k: (float(ms[i]), int(ln[i])) for i, k in enumerate(("kb_gradient", "kb_face", "kb_update"))}
+
+    def stream(self) -> int:
+        return int(library().fv2d_batch_stream(self.h) or 0)

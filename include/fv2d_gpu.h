@@ -152,6 +152,38 @@ long long fv2d_device_bytes(fv2d_handle* h);
 
 const char* fv2d_last_error(fv2d_handle* h);   /* h may be NULL: last creation error */
 
+/* ---- batched solves (many independent solves resident on one GPU) ----------------------------
+ * No single counterpart in the reference, which runs one solve per process; each solve in a batch
+ * advances exactly as ssp_rk3() (src/solver/ssp_rk3.cpp:18) would advance it alone.  A batch owns
+ * one device arena sized at creation (cells, faces, solves); solves are added (mesh + case, the
+ * same inputs as fv2d_create) and removed between iterations; fv2d_batch_step advances every
+ * active solve together with one persistent launch per kernel per RK stage, replayed as one CUDA
+ * graph per iteration.  Per-solve residual L2 norms of the last iteration support retirement.
+ * Errors: fv2d_last_error(NULL).                                                                 */
+typedef struct fv2d_batch fv2d_batch;
+int fv2d_batch_create(long long max_cells, long long max_faces, int max_solves, int precision, fv2d_batch** out);
+void fv2d_batch_destroy(fv2d_batch* b);
+/* device bytes a solve with this mesh occupies in a batch of the given precision (admission)   */
+int fv2d_batch_footprint(const fv2d_mesh_desc* desc, int precision, long long* bytes);
+/* FV2D_ERR_NOMEM when the arena has no room (the batch is unchanged)                           */
+int fv2d_batch_add(fv2d_batch* b, const fv2d_mesh_desc* desc, const fv2d_case* cs, int* solve_id);
+int fv2d_batch_remove(fv2d_batch* b, int solve_id);
+int fv2d_batch_step(fv2d_batch* b, int iterations);
+/* for every active solve: id, the 4 residual L2 norms of its last iteration, iterations done   */
+int fv2d_batch_norms(fv2d_batch* b, int* solve_ids, double* norms4, int* iterations, int max, int* n);
+int fv2d_batch_get_state(fv2d_batch* b, int solve_id, double* q);
+int fv2d_batch_synchronize(fv2d_batch* b);
+/* tile shape: threads per block, tile = block * tile_mult[bucket] elements; buckets split at
+ * bucket_edges[0] and bucket_edges[1] cells                                                     */
+int fv2d_batch_set_tuning(fv2d_batch* b, int block, const int* tile_mult3, const int* bucket_edges2);
+int fv2d_batch_get_tuning(fv2d_batch* b, int* block, int* tile_mult3, int* bucket_edges2);
+/* cells used/capacity, faces used/capacity, incidences used/capacity, active solves, bytes      */
+int fv2d_batch_usage(fv2d_batch* b, long long* out8);
+int fv2d_batch_set_kernel_timing(fv2d_batch* b, int enable);
+/* totals since timing was enabled for gradient, face and update kernels                        */
+int fv2d_batch_kernel_times(fv2d_batch* b, double* ms3, int* launches3);
+void* fv2d_batch_stream(fv2d_batch* b);
+
 /* ---- residual without allocation ----------------------------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device memory: a host
  * application whose own allocator has reserved the GPU's memory up front (a cudaMalloc here would

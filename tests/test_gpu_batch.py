@@ -1,0 +1,106 @@
+"""Batched solves: each solve advances exactly as it would alone (bit for bit: the batch kernels
+run the same per-element code), solves can join and leave between iterations, tile shapes do not
+change results, and admission refuses what does not fit."""
+import numpy as np
+import pytest
+
+from conftest import bits_equal, max_rel
+
+pytestmark = pytest.mark.gpu
+
+
+def mix(pkg):
+    mg = pkg.meshgen
+    base = dict(mg.DEFAULT_CASE)
+    return [
+        (mg.voronoi_bump_channel(6000, seed=1),
+         dict(base, eqn="EULER", limiter="SQUEEZE", time_step_type="GLOBAL", CFL=0.8, u=mg.mach_speed(0.7))),
+        (mg.voronoi_cylinder(9000, seed=2, box=(6.0, 3.0), h_wall=0.01, h_far=0.08),
+         dict(base, eqn="NS", mu=0.02, limiter="SQUEEZE", time_step_type="LOCAL", CFL=0.5, BC1="NO_SLIP_WALL",
+              BC2="FREESTREAM", u=mg.mach_speed(0.3), v=8.0)),
+        (mg.channel_bump_quads(48, 24),
+         dict(base, eqn="EULER", solution_poly_order=0, limiter="NONE", time_step_type="LOCAL", CFL=0.9,
+              u=mg.mach_speed(0.5))),
+        (mg.voronoi_bump_channel(3000, seed=5, thickness=0.06),
+         dict(base, eqn="NS", mu=0.01, limiter="NONE", time_step_type="GLOBAL", CFL=0.5, BC1="NO_SLIP_WALL",
+              BC2="EXTRAPOLATION", u=mg.mach_speed(0.4))),
+    ]
+
+
+def alone(pkg, grid, case, iters, precision):
+    s = pkg.Solver(grid, case, precision=precision)
+    s.step(iters)
+    q = s.get_state()
+    r = s.residual_norm()
+    s.close()
+    return q, r
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_batch_equals_alone(pkg, precision):
+    prec = pkg.FP64 if precision == "fp64" else pkg.FP32
+    cases = mix(pkg)
+    b = pkg.Batch(200000, 600000, 16, precision=prec)
+    ids = [b.add(g, c) for g, c in cases]
+    b.step(6)
+    norms = b.norms()
+    for sid, (g, c) in zip(ids, cases):
+        q_alone, r_alone = alone(pkg, g, c, 6, prec)
+        q = b.get_state(sid)
+        assert bits_equal(q, q_alone), f"solve {sid}: max rel {max_rel(q, q_alone):.2e}"
+        nr, it = norms[sid]
+        assert it == 6
+        assert np.allclose(nr, r_alone, rtol=1e-9 if prec == pkg.FP64 else 1e-5, atol=0)
+    b.close()
+
+
+def test_batch_join_and_leave(pkg):
+    cases = mix(pkg)
+    b = pkg.Batch(200000, 600000, 8, precision=pkg.FP64)
+    a = b.add(*cases[0])
+    c = b.add(*cases[1])
+    b.step(2)
+    d = b.add(*cases[2])          # joins after 2 iterations
+    b.step(1)
+    b.remove(c)                    # leaves after 3 iterations
+    e = b.add(*cases[3])           # reuses the freed ranges
+    b.step(3)
+    expect = {a: (cases[0], 6), d: (cases[2], 4), e: (cases[3], 3)}
+    norms = b.norms()
+    assert set(norms) == set(expect)
+    for sid, ((g, cs), iters) in expect.items():
+        q_alone, _ = alone(pkg, g, cs, iters, pkg.FP64)
+        assert bits_equal(b.get_state(sid), q_alone), sid
+        assert norms[sid][1] == iters
+    b.close()
+
+
+def test_batch_tuning_does_not_change_results(pkg):
+    cases = mix(pkg)[:2]
+    results = []
+    for block, mult in ((256, (1, 2, 4)), (128, (1, 1, 1)), (512, (4, 8, 2))):
+        b = pkg.Batch(100000, 300000, 4, precision=pkg.FP64)
+        b.set_tuning(block, mult, (4000, 8000))
+        ids = [b.add(g, c) for g, c in cases]
+        b.step(4)
+        results.append([b.get_state(i) for i in ids])
+        b.close()
+    for r in results[1:]:
+        for x, y in zip(results[0], r):
+            assert bits_equal(x, y)
+
+
+def test_batch_admission(pkg):
+    g, c = mix(pkg)[0]
+    need = pkg.Batch.footprint(g, pkg.FP32)
+    assert need > 0
+    b = pkg.Batch(g.num_cells + 10, g.num_faces + 10, 4, precision=pkg.FP32)
+    b.add(g, c)
+    with pytest.raises(pkg.Fv2dError) as e:
+        b.add(g, c)                # no room left: refused, batch unchanged
+    assert e.value.code == 6
+    u = b.usage()
+    assert u["active"] == 1 and u["cells_used"] == g.num_cells + 1
+    b.step(2)
+    assert len(b.norms()) == 1
+    b.close()
