@@ -108,10 +108,13 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def bytes_per_launch(kernel, N, F, ninc, Nb, s, ns, squeeze, stage_avg=True):
-    """Algorithmic bytes of one launch: every array element the kernel must touch, counted once.
-    s = state bytes (8 FP64, 4 FP32); integers 4 B; LSQ moments always 8 B."""
-    if kernel == "k_gradient":
+def bytes_per_launch(kernel, N, F, ninc, Nb, s, ns, squeeze, comp=False, store_r=True, order2=True):
+    """Algorithmic bytes of one launch (average over the three RK stages): every array element the
+    kernel must touch, counted once.  s = state bytes (8 FP64, 4 FP32); ids 4 B; LSQ moments 8 B.
+    comp: FP32 delta-form increments and compensated base state; store_r: residual kept (last stage)."""
+    if kernel in ("k_gradient", "kb_gradient"):
+        if not order2:
+            return 0.0
         b = N * (4 * s + 8 * s)                  # Q read, G write
         if squeeze:
             b += N * (4 * s + 8 * s)             # previous Q and limited G
@@ -119,32 +122,39 @@ def bytes_per_launch(kernel, N, F, ninc, Nb, s, ns, squeeze, stage_avg=True):
         b += F * s * (6 if squeeze else 2)       # dxj, dyj (+ c1dx, c1dy, c2dx, c2dy)
         b += Nb * 2 * s                          # nx, ny on boundary faces
         return b
-    if kernel == "k_face":
-        geo = 9 + (5 if ns else 0)
+    if kernel in ("k_face", "kb_face"):
+        geo = 9 + (5 if (ns and order2) else 0)
         b = F * (8 + geo * s)                    # c1, c2, geometry
-        b += N * (4 * s + 8 * s)                 # Q and G of every cell
+        b += N * (4 * s + (8 * s if order2 else 0))   # Q (and G) of every cell
         b += F * 4 * s                           # t written
-        b += (F * s) / 3.0 if stage_avg else 0   # spectral term, last stage only
+        b += (F * s) / 3.0                       # spectral term, last stage only
         return b
-    if kernel == "k_update":
+    if kernel in ("k_update", "kb_update"):
         b = N * 4 + ninc * 4 + F * 4 * s         # CSR, face contributions
         b += N * s                               # volume
-        b += N * 4 * s * (1 + 2.0 / 3.0)         # Qn read; Q1/Q2 read on stages 2-3
-        b += N * 4 * s                           # new state written
-        b += N * s * (1 + 2.0 / 3.0) / 1.0       # dt written (stage 1) / read (stages 2-3)
-        b += (N * 4 * s) / 3.0                   # residual stored on the last stage
+        b += N * 4 * s                           # Qn read
+        b += N * 4 * s                           # stage result written
+        b += N * s                               # dt written (stage 1) or read (stages 2-3)
         b += (F * s + N * s) / 3.0               # spectral sum (last stage)
+        if comp:
+            b += N * 4 * s * (1 + 2 + 1) / 3.0   # increment D: write, read+write, read
+            b += N * 4 * s * 2 / 3.0             # compensation term: read+write on the last stage
+        else:
+            b += N * 4 * s * 2.0 / 3.0           # Q1 / Q2 read on stages 2-3
+        if store_r:
+            b += (N * 4 * s) / 3.0               # residual stored on the last stage
         return b
     return 0.0
 
 
-def roofline(kt, N, F, ninc, Nb, s, ns, squeeze, peak):
+def roofline(kt, kbytes, peak):
+    """Dominant kernel (largest total time) of the event-timed pass, its achieved GB/s on the
+    algorithmic bytes, and every kernel's share of the stage time."""
     per = {}
-    for k in ("k_gradient", "k_face", "k_update"):
+    for k, nbytes in kbytes.items():
         ms, launches = kt.get(k, (0.0, 0))
         if launches:
-            per[k] = dict(avg_ms=ms / launches, launches=launches, total_ms=ms,
-                          bytes=bytes_per_launch(k, N, F, ninc, Nb, s, ns, squeeze))
+            per[k] = dict(avg_ms=ms / launches, launches=launches, total_ms=ms, bytes=nbytes)
     tot = sum(v["total_ms"] for v in per.values()) or 1.0
     dom = max(per, key=lambda k: per[k]["total_ms"])
     d = per[dom]
@@ -229,6 +239,88 @@ def run_reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def single_kernel_bytes(N, F, ninc, Nb, s, comp, store_r=True):
+    return {k: bytes_per_launch(k, N, F, ninc, Nb, s, True, True, comp=comp, store_r=store_r)
+            for k in ("k_gradient", "k_face", "k_update")}
+
+
+def measure_fp32(pkg, grid, case, args, peak, peak_kind, N, F, ninc, Nb):
+    """The same solve through the FP32 path: device-timed throughput and its dominant kernel."""
+    import torch
+    s = pkg.Solver(grid, case, precision=pkg.FP32)
+    st = torch.cuda.ExternalStream(s.stream())
+    s.step(args.warmup)
+    s.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(args.steps):
+        s.step(1)
+    e1.record(st)
+    e1.synchronize()
+    s.synchronize()
+    ms = e0.elapsed_time(e1)
+    s.set_kernel_timing(True)
+    s.step(args.steps)
+    kt = s.kernel_times()
+    s.close()
+    dom, roof, per = roofline(kt, single_kernel_bytes(N, F, ninc, Nb, 4, True), peak)
+    roof["peak_source"] = f"{peak_kind} hbm_gbs"
+    roof["traffic"] = ncu_traffic("fp32", dom, N, F)
+    return {"value": 3.0 * N * args.steps / (ms * 1e-3), "unit": "cell-stage/s", "ms_per_step": ms / args.steps,
+            "roofline": roof,
+            "kernels": {k: {"avg_ms": round(v["avg_ms"], 4), "gbs": round(v["bytes"] / (v["avg_ms"] * 1e-3) / 1e9, 1)}
+                        for k, v in per.items()}}
+
+
+def measure_batched(pkg, args, peak, peak_kind):
+    """c4: 256 independent FP32 solves in one batch, tile shapes autotuned, graph-replayed iterations."""
+    import torch
+    from fv2d_gb300 import autotune, workloads
+    t0 = time.time()
+    specs = workloads.c4_specs(args.batch_solves, seed=args.seed)
+    grids = workloads.grids_parallel(specs)
+    t_gen = time.time() - t0
+    tot_c = sum(g.num_cells for g in grids)
+    tot_f = sum(g.num_faces for g in grids)
+    b = pkg.Batch(tot_c + 16, tot_f + 16, len(grids) + 1, precision=pkg.FP32)
+    t0 = time.time()
+    for g, sp in zip(grids, specs):
+        b.add(g, workloads.spec_case(sp))
+    t_add = time.time() - t0
+    tuning = autotune.tune(b, iters=3, warmup=1)
+    st = torch.cuda.ExternalStream(b.stream())
+    b.step(args.warmup)
+    b.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    b.step(args.steps)
+    e1.record(st)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    b.set_kernel_timing(True)
+    b.step(max(3, args.steps // 4))
+    kt = b.kernel_times()
+    b.set_kernel_timing(False)
+    kbytes = {"kb_gradient": 0.0, "kb_face": 0.0, "kb_update": 0.0}
+    for g, sp in zip(grids, specs):
+        nb = int((g.fc2 <= 0).sum())
+        for k in kbytes:
+            kbytes[k] += bytes_per_launch(k, g.num_cells, g.num_faces, 2 * g.num_faces - nb, nb, 4, sp["ns"], True,
+                                          comp=True, store_r=False)
+    dom, roof, per = roofline(kt, kbytes, peak)
+    roof["peak_source"] = f"{peak_kind} hbm_gbs"
+    norms = b.norms()
+    finite = all(np.all(np.isfinite(v[0])) for v in norms.values())
+    b.close()
+    return {"value": 3.0 * tot_c * args.steps / (ms * 1e-3), "unit": "cell-stage/s", "ms_per_step": ms / args.steps,
+            "solves": len(grids), "cells": tot_c, "faces": tot_f, "ns_solves": sum(sp["ns"] for sp in specs),
+            "roofline": roof, "tuning": {k: tuning[k] for k in ("block", "tile_mult", "bucket_edges")},
+            "kernels": {k: {"avg_ms": round(v["avg_ms"], 4), "gbs": round(v["bytes"] / (v["avg_ms"] * 1e-3) / 1e9, 1)}
+                        for k, v in per.items()},
+            "finite": finite, "mesh_gen_s": round(t_gen, 1), "admit_s": round(t_add, 1),
+            "workload": "256 bump-channel Voronoi solves, cells log-uniform 2k-200k, FP32, one graph per iteration"}
+
+
 def run_gpu_arm(args):
     import torch
 
@@ -240,8 +332,7 @@ def run_gpu_arm(args):
         dist.init_process_group("gloo")
     torch.cuda.set_device(local)
     t_mesh = time.time()
-    grid = make_grid(pkg, args.cells)
-    case = workload_case(pkg, args.cells)
+    grid, case = make_grid(pkg, args.cells), workload_case(pkg, args.cells)
     t_mesh = time.time() - t_mesh
     prec = pkg.FP64 if args.precision == "fp64" else pkg.FP32
     N, F = grid.num_cells, grid.num_faces
@@ -288,10 +379,9 @@ def run_gpu_arm(args):
     kt = solver.kernel_times()
     solver.set_kernel_timing(False)
     peak, peak_kind = peaks()
-    dom, roof, per = roofline(kt, N, F, ninc, Nb, s_bytes, True, True, peak)
+    dom, roof, per = roofline(kt, single_kernel_bytes(N, F, ninc, Nb, s_bytes, prec == pkg.FP32), peak)
     roof["peak_source"] = f"{peak_kind} hbm_gbs"
     roof["traffic"] = ncu_traffic(args.precision, dom, N, F)
-    launches = sum(v[1] for k, v in kt.items() if k in ("k_gradient", "k_face", "k_update"))
     gpu_launches = 3 * 3 * args.steps
 
     # ---- end to end through the C ABI with host buffers: upload Qbar, one iteration, download
@@ -307,6 +397,16 @@ def run_gpu_arm(args):
     t_e2e = time.perf_counter() - t0
     e2e = {"value": ws * 3.0 * N * args.steps / t_e2e, "unit": "cell-stage/s",
            "h2d_bytes_per_step": 4 * 8 * N, "d2h_bytes_per_step": 4 * 8 * N + 4 * 8}
+    dev_bytes = solver.device_bytes()
+    solver.close()
+
+    fp32 = None
+    if rank == 0 and prec == pkg.FP64 and not args.no_fp32:
+        fp32 = measure_fp32(pkg, grid, case, args, peak, peak_kind, N, F, ninc, Nb)
+    batched = None
+    if rank == 0 and not args.no_batch:
+        batched = measure_batched(pkg, args, peak, peak_kind)
+        batched["vs_fp64_plain"] = round(batched["value"] / value * ws, 2)
 
     # ---- CPU baseline (oracle port, 1 core, bounded sample)
     cpu = None
@@ -330,9 +430,9 @@ def run_gpu_arm(args):
                 "kernels": {k: {"avg_ms": round(v["avg_ms"], 4), "launches": v["launches"],
                                 "bytes_per_launch": int(v["bytes"]),
                                 "gbs": round(v["bytes"] / (v["avg_ms"] * 1e-3) / 1e9, 1)} for k, v in per.items()},
-                "residual_norm": [float(x) for x in norm], "device_bytes": solver.device_bytes()}
+                "fp32": fp32, "batched": batched,
+                "residual_norm": [float(x) for x in norm], "device_bytes": dev_bytes}
         print(json.dumps(line), flush=True)
-    solver.close()
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
@@ -349,6 +449,10 @@ def main():
     ap.add_argument("--cpu-iters", type=int, default=4)
     ap.add_argument("--cpu-cores", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp32", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-solves", type=int, default=256)
+    ap.add_argument("--seed", type=int, default=0)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -1,0 +1,54 @@
+"""Autotuner of the batched engine's tile shapes.
+
+The batch kernels are persistent grids over tiles of `block * mult[bucket]` cells or faces of one
+solve (buckets split by solve size).  The tuner times whole iterations of the loaded batch (CUDA
+graph replay, wall clock around synchronised steps) for: first the block size with unit tiles,
+then each size bucket's tile multiple in turn, keeping the fastest.  Tile shapes never change
+results (the per-element code is the same), so tuning can run on the live batch.
+"""
+from __future__ import annotations
+
+import time
+
+BLOCKS = (128, 256, 512)
+MULTS = (1, 2, 4, 8)
+
+
+def time_iterations(batch, iters=5, warmup=2):
+    batch.step(warmup)
+    batch.synchronize()
+    t0 = time.perf_counter()
+    batch.step(iters)
+    batch.synchronize()
+    return (time.perf_counter() - t0) / iters
+
+
+def tune(batch, iters=5, warmup=2, blocks=BLOCKS, mults=MULTS, edges=None, log=None):
+    """Pick the fastest (block, tile_mult per bucket) for the solves currently in `batch`."""
+    _, mult0, edges0 = batch.get_tuning()
+    edges = tuple(edges or edges0)
+    trials = []
+    best = None
+    for b in blocks:
+        batch.set_tuning(b, (1, 1, 1), edges)
+        t = time_iterations(batch, iters, warmup)
+        trials.append(((b, (1, 1, 1)), t))
+        if best is None or t < best[1]:
+            best = ((b, [1, 1, 1]), t)
+    block, mult = best[0]
+    for bucket in range(3):
+        for m in mults[1:]:
+            trial = list(mult)
+            trial[bucket] = m
+            batch.set_tuning(block, tuple(trial), edges)
+            t = time_iterations(batch, iters, warmup)
+            trials.append(((block, tuple(trial)), t))
+            if t < best[1]:
+                best = ((block, trial), t)
+                mult = trial
+    batch.set_tuning(block, tuple(mult), edges)
+    if log:
+        for (cfg, t) in trials:
+            log(f"autotune block={cfg[0]} mult={cfg[1]}: {t * 1e3:.3f} ms/iteration")
+    return dict(block=block, tile_mult=list(mult), bucket_edges=list(edges), ms_per_iteration=best[1] * 1e3,
+                trials=[dict(block=c[0], tile_mult=list(c[1]), ms=t * 1e3) for c, t in trials])
