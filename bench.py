@@ -287,7 +287,11 @@ def measure_batched(pkg, args, peak, peak_kind):
     for g, sp in zip(grids, specs):
         b.add(g, workloads.spec_case(sp))
     t_add = time.time() - t0
-    tuning = autotune.tune(b, iters=3, warmup=1)
+    if args.no_tune:
+        b.set_tuning(256, (1, 2, 4), (16384, 131072))
+        tuning = {"block": 256, "tile_mult": [1, 2, 4], "bucket_edges": [16384, 131072]}
+    else:
+        tuning = autotune.tune(b, iters=3, warmup=1)
     st = torch.cuda.ExternalStream(b.stream())
     b.step(args.warmup)
     b.synchronize()
@@ -319,6 +323,23 @@ def measure_batched(pkg, args, peak, peak_kind):
                         for k, v in per.items()},
             "finite": finite, "mesh_gen_s": round(t_gen, 1), "admit_s": round(t_add, 1),
             "workload": "256 bump-channel Voronoi solves, cells log-uniform 2k-200k, FP32, one graph per iteration"}
+
+
+def run_partial(args):
+    """One measurement alone (profiling runs): --only fp32 | batched."""
+    import torch
+    pkg = entry.load_package()
+    pkg.build.build()
+    torch.cuda.set_device(0)
+    peak, peak_kind = peaks()
+    if args.only == "fp32":
+        grid, case = make_grid(pkg, args.cells), workload_case(pkg, args.cells)
+        N, F = grid.num_cells, grid.num_faces
+        Nb = int((grid.fc2 <= 0).sum())
+        out = measure_fp32(pkg, grid, case, args, peak, peak_kind, N, F, 2 * F - Nb, Nb)
+    else:
+        out = measure_batched(pkg, args, peak, peak_kind)
+    print(json.dumps({"only": args.only, **out}), flush=True)
 
 
 def run_gpu_arm(args):
@@ -453,11 +474,15 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--batch-solves", type=int, default=256)
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--only", default="all", choices=["all", "fp32", "batched"])
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference_arm(args)
+    elif args.only != "all":
+        run_partial(args)
     else:
         run_gpu_arm(args)
 
