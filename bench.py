@@ -119,7 +119,7 @@ def bytes_per_launch(kernel, N, F, ninc, Nb, s, ns, squeeze, comp=False, store_r
         if squeeze:
             b += N * (4 * s + 8 * s)             # previous Q and limited G
         b += N * 4 + ninc * 8 + N * 24           # CSR offsets, (face, neighbour) pairs, Ixx/Iyy/Ixy
-        b += F * s * (6 if squeeze else 2)       # dxj, dyj (+ c1dx, c1dy, c2dx, c2dy)
+        b += ninc * 4 * s                        # per-incidence dxj, dyj, face-centre offset
         b += Nb * 2 * s                          # nx, ny on boundary faces
         return b
     if kernel in ("k_face", "kb_face"):
@@ -318,7 +318,7 @@ def measure_batched(pkg, args, peak, peak_kind):
     b.close()
     return {"value": 3.0 * tot_c * args.steps / (ms * 1e-3), "unit": "cell-stage/s", "ms_per_step": ms / args.steps,
             "solves": len(grids), "cells": tot_c, "faces": tot_f, "ns_solves": sum(sp["ns"] for sp in specs),
-            "roofline": roof, "tuning": {k: tuning[k] for k in ("block", "tile_mult", "bucket_edges")},
+            "roofline": roof, "tuning": {k: tuning.get(k) for k in ("block", "tile_mult", "bucket_edges", "full_grid")},
             "kernels": {k: {"avg_ms": round(v["avg_ms"], 4), "gbs": round(v["bytes"] / (v["avg_ms"] * 1e-3) / 1e9, 1)}
                         for k, v in per.items()},
             "finite": finite, "mesh_gen_s": round(t_gen, 1), "admit_s": round(t_add, 1),

@@ -27,6 +27,7 @@ def tune(batch, iters=5, warmup=2, blocks=BLOCKS, mults=MULTS, edges=None, log=N
     """Pick the fastest (block, tile_mult per bucket) for the solves currently in `batch`."""
     _, mult0, edges0 = batch.get_tuning()
     edges = tuple(edges or edges0)
+    batch.set_grid_mode(False)
     trials = []
     best = None
     for b in blocks:
@@ -47,8 +48,19 @@ def tune(batch, iters=5, warmup=2, blocks=BLOCKS, mults=MULTS, edges=None, log=N
                 best = ((block, trial), t)
                 mult = trial
     batch.set_tuning(block, tuple(mult), edges)
+    # grid mode: persistent (SMs x resident blocks) against one block per tile
+    full = False
+    batch.set_grid_mode(True)
+    t = time_iterations(batch, iters, warmup)
+    trials.append(((block, tuple(mult), "full-grid"), t))
+    if t < best[1]:
+        best = ((block, mult), t)
+        full = True
+    else:
+        batch.set_grid_mode(False)
     if log:
         for (cfg, t) in trials:
             log(f"autotune block={cfg[0]} mult={cfg[1]}: {t * 1e3:.3f} ms/iteration")
-    return dict(block=block, tile_mult=list(mult), bucket_edges=list(edges), ms_per_iteration=best[1] * 1e3,
-                trials=[dict(block=c[0], tile_mult=list(c[1]), ms=t * 1e3) for c, t in trials])
+    return dict(block=block, tile_mult=list(mult), bucket_edges=list(edges), full_grid=full,
+                ms_per_iteration=best[1] * 1e3,
+                trials=[dict(block=c[0], tile_mult=list(c[1]), full_grid=len(c) > 2, ms=t * 1e3) for c, t in trials])

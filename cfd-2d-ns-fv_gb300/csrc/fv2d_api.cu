@@ -330,6 +330,13 @@ int fv2d_batch_get_tuning(fv2d_batch* b, int* block, int* tile_mult3, int* bucke
     return FV2D_OK;
 }
 
+int fv2d_batch_set_grid_mode(fv2d_batch* b, int full_grid) {
+    FV2D_BH(b);
+    fv2d::BatchTuning t = b->b->tuning();
+    t.full_grid = full_grid != 0;
+    FV2D_BRET(b, b->b->set_tuning(t));
+}
+
 int fv2d_batch_usage(fv2d_batch* b, long long* out8) {
     FV2D_BH(b);
     if (!out8) return fail(FV2D_ERR_ARG, "null output");
@@ -353,6 +360,6 @@ void batch_footprint(int precision, long long cells, long long faces, long long 
     const long long s = precision == FV2D_FP64 ? 8 : 4;
     const long long cell = (precision == FV2D_FP64 ? 9 : 11) * 4 * s + 3 * s + 24 + 4;   // Q[3], G[3], (D, lo), dt, S, vol, LSQ, offsets
     const long long face = 3 * 4 + 14 * s + 4 * s + s;        // ids, geometry, contribution, spectral term
-    *bytes = (cells + 1) * cell + faces * face + incs * 8;
+    *bytes = (cells + 1) * cell + faces * face + incs * (8 + 4 * s);
 }
 }  // namespace fv2d

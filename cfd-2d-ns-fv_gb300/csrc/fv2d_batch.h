@@ -15,6 +15,7 @@ struct BatchTuning {
     int block = 256;              // threads per block of the persistent kernels
     int tile_mult[3] = {1, 2, 4}; // tile = block * mult elements, per size bucket (small, medium, large)
     int bucket_edges[2] = {16384, 131072};   // cells
+    int full_grid = 0;            // 0: persistent grid (SMs x resident blocks); 1: one block per tile
 };
 
 class Batch {

@@ -63,7 +63,7 @@ __device__ __forceinline__ T block_max_t(T v, T* red) {
 }
 
 template <class T>
-__global__ void __launch_bounds__(512)
+__global__ void __launch_bounds__(512, sizeof(T) == 4 ? 2 : 1)
 kb_gradient(const Tile* __restrict__ tiles, const int* __restrict__ ntiles, DevMesh<T> m,
             const SolveParams<T>* __restrict__ P, const Q4<T>* __restrict__ Qin, const Q4<T>* __restrict__ Qprev,
             const Q4<T>* __restrict__ Gprev, Q4<T>* __restrict__ Gout) {
@@ -87,7 +87,7 @@ kb_gradient(const Tile* __restrict__ tiles, const int* __restrict__ ntiles, DevM
 }
 
 template <class T, bool LAST>
-__global__ void __launch_bounds__(512)
+__global__ void __launch_bounds__(512, sizeof(T) == 4 ? 2 : 1)
 kb_face(const Tile* __restrict__ tiles, const int* __restrict__ ntiles, DevMesh<T> m,
         const SolveParams<T>* __restrict__ P, const Q4<T>* __restrict__ Qin, const Q4<T>* __restrict__ G,
         Q4<T>* __restrict__ tout, T* __restrict__ sout) {
@@ -233,7 +233,7 @@ public:
         for (int i = 0; i < 3; i++) og[i] = take(2 * q4 * Nc_);
         size_t odt = take(sizeof(T) * Nc_), oS = take(sizeof(T) * Nc_), ovol = take(sizeof(T) * Nc_);
         size_t oixx = take(8 * Nc_), oiyy = take(8 * Nc_), oixy = take(8 * Nc_), ooff = take(4 * Nc_);
-        size_t oinc = take(4 * Ic_), onbr = take(4 * Ic_);
+        size_t oinc = take(4 * Ic_), onbr = take(4 * Ic_), oigeo = take(q4 * Ic_);
         size_t ofc1 = take(4 * Fc_), ofc2 = take(4 * Fc_), oqc = take(4 * Fc_);
         size_t ogeo[14];
         for (int gI = 0; gI < 14; gI++) ogeo[gI] = take(sizeof(T) * Fc_);
@@ -260,6 +260,7 @@ public:
         D_ = comp ? (Q4<T>*)(a + oD) : nullptr;
         Qlo_ = comp ? (Q4<T>*)(a + olo) : nullptr;
         m_.inc_off = incoff; m_.inc = inc; m_.nbr = nbr; m_.fc1 = fc1; m_.fc2 = fc2; m_.qcell = qc;
+        m_.igeo = (const Q4<T>*)(a + oigeo);
         m_.g.nx = geo_[0]; m_.g.ny = geo_[1]; m_.g.area = geo_[2]; m_.g.c1dx = geo_[3]; m_.g.c1dy = geo_[4];
         m_.g.c2dx = geo_[5]; m_.g.c2dy = geo_[6]; m_.g.dxj = geo_[7]; m_.g.dyj = geo_[8]; m_.g.mx = geo_[9];
         m_.g.my = geo_[10]; m_.g.lx = geo_[11]; m_.g.ly = geo_[12]; m_.g.dist = geo_[13];
@@ -312,6 +313,7 @@ public:
         if ((rc = put(m_.Iyy + r.c0, L.Iyy.data(), 8 * n))) return rc;
         if ((rc = put(m_.Ixy + r.c0, L.Ixy.data(), 8 * n))) return rc;
         if ((rc = putT((T*)m_.vol + r.c0, L.vol))) return rc;
+        if ((rc = putT((T*)m_.igeo + 4 * r.i0, L.igeo))) return rc;
         for (int gI = 0; gI < 14; gI++) if ((rc = putT(geo_[gI] + r.f0, L.fgeo[gI]))) return rc;
         // parameters and the uniform freestream state (main.cpp:75-118)
         SolveParams<T> p{};
@@ -506,6 +508,10 @@ private:
         if ((rc = put(cnt_, cnt, sizeof(cnt)))) return rc;
         n_ctiles_ = cnt[0];
         n_ftiles_ = cnt[1];
+        if (tune_.full_grid) {   // grid sizes are baked into the captured graph
+            compute_grids();
+            if (graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
+        }
         return FV2D_OK;
     }
 
@@ -531,6 +537,11 @@ private:
         return std::max(1, per) * sms_;
     }
     void compute_grids() {
+        if (tune_.full_grid) {   // one block per tile: grids follow the tile counts
+            gg_ = gu_[0] = gu_[1] = gu_[2] = std::max(1, n_ctiles_);
+            gf_[0] = gf_[1] = std::max(1, n_ftiles_);
+            return;
+        }
         gg_ = grid_for((const void*)kb_gradient<T>);
         gf_[0] = grid_for((const void*)kb_face<T, false>);
         gf_[1] = grid_for((const void*)kb_face<T, true>);

@@ -394,7 +394,7 @@ void build_layout(const HostMesh& m, DeviceLayout& L) {
         L.inc_off[i + 1] = L.inc_off[i] + (m.cf_off[o + 1] - m.cf_off[o]);
     }
     L.ninc = L.inc_off[nc];
-    L.inc.resize(L.ninc); L.nbr.resize(L.ninc);
+    L.inc.resize(L.ninc); L.nbr.resize(L.ninc); L.igeo.resize(4 * (size_t)L.ninc);
     for (int i = 0; i < nc; i++) {
         const int o = m.cell_new2old[i];
         int w = L.inc_off[i];
@@ -402,6 +402,10 @@ void build_layout(const HostMesh& m, DeviceLayout& L) {
             const int f = m.cf[k];
             const int side = (m.fc1[f] == o) ? 0 : 1;
             L.inc[w] = (m.face_old2new[f] << 1) | side;
+            L.igeo[4 * (size_t)w + 0] = m.dxj[f];
+            L.igeo[4 * (size_t)w + 1] = m.dyj[f];
+            L.igeo[4 * (size_t)w + 2] = side == 0 ? m.c1dx[f] : m.c2dx[f];
+            L.igeo[4 * (size_t)w + 3] = side == 0 ? m.c1dy[f] : m.c2dy[f];
             if (side == 0) L.nbr[w] = m.fc2[f] >= 0 ? m.cell_old2new[m.fc2[f]] : m.fc2[f];
             else L.nbr[w] = m.cell_old2new[m.fc1[f]];
         }

@@ -36,6 +36,8 @@ struct DeviceLayout {
     std::vector<int> inc_off;               // [nc+1]
     std::vector<int> inc;                   // [ninc] (new face id << 1) | side, ascending original face id
     std::vector<int> nbr;                   // [ninc] neighbour (new id) or BC code
+    std::vector<double> igeo;               // [4 ninc] per incidence: dxj, dyj, and the face-centre offset
+                                            //   from this cell (c1dx, c1dy or c2dx, c2dy), CSR order
     std::vector<int> fc1, fc2;              // [nf]   new cell ids / BC code
     std::vector<int> qcell;                 // [nf]   NO_SLIP gradient ghost cell (new id of cell `orig face id`), else -1
     std::vector<double> vol, Ixx, Iyy, Ixy; // [nc]

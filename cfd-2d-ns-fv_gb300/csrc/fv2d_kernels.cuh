@@ -41,6 +41,7 @@ struct FaceGeo {
 template <class T>
 struct DevMesh {
     const int *inc_off, *inc, *nbr, *fc1, *fc2, *qcell;
+    const Q4<T>* igeo;   // per incidence (CSR order): dxj, dyj, offset of the face centre from the cell
     FaceGeo<T> g;
     const double *Ixx, *Iyy, *Ixy;
     const T* vol;
@@ -142,7 +143,8 @@ __device__ __forceinline__ void gradient_cell(int c, const DevMesh<T>& m, const 
 #pragma unroll
                 for (int j = 0; j < 4; j++) { qmin[j] = min2(qmin[j], qc.p[j]); qmax[j] = max2(qmax[j], qc.p[j]); }
         }
-        const T fx = g.dxj[f], fy = g.dyj[f];
+        const Q4<T> ig = ldq(m.igeo, i);
+        const T fx = ig.p[0], fy = ig.p[1];
 #pragma unroll
         for (int j = 0; j < 4; j++) { sx[j] += d[j] * fx; sy[j] += d[j] * fy; }
     }
@@ -158,9 +160,8 @@ __device__ __forceinline__ void gradient_cell(int c, const DevMesh<T>& m, const 
         Q4<T> qp, gpx, gpy;
         if (!first_stage) { qp = ldq(Qprev, c); gpx = ldq(Gprev, 2 * c); gpy = ldq(Gprev, 2 * c + 1); }
         for (int i = b; i < e; i++) {
-            const int f = inc[i] >> 1, side = inc[i] & 1;
-            const T dx = side == 0 ? g.c1dx[f] : g.c2dx[f];
-            const T dy = side == 0 ? g.c1dy[f] : g.c2dy[f];
+            const Q4<T> ig = ldq(m.igeo, i);
+            const T dx = ig.p[2], dy = ig.p[3];
 #pragma unroll
             for (int j = 0; j < 4; j++) {
                 const T qf = first_stage ? T(-101) : qp.p[j] + gpx.p[j] * dx + gpy.p[j] * dy;
@@ -177,8 +178,10 @@ __device__ __forceinline__ void gradient_cell(int c, const DevMesh<T>& m, const 
     Gout[2 * c + 1] = gy;
 }
 
+// Occupancy: the FP32 kernels are latency-bound gathers, so their register use is capped for more
+// resident warps; the FP64 kernels are FP64-ALU-bound and keep their registers.
 template <class T, bool SQUEEZE>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 5 : 1)
 k_gradient(int nc, DevMesh<T> m, const Q4<T>* __restrict__ Q, const Q4<T>* __restrict__ Qprev,
            const Q4<T>* __restrict__ Gprev, Q4<T>* __restrict__ Gout, Consts<T> k, int first_stage, int init_prims) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -266,7 +269,9 @@ __device__ __forceinline__ void face_flux(int f, const DevMesh<T>& m, const Q4<T
         bool have = true;
         if (c2 >= 0) {
             const T ad = fabs(g.dist[f]);
-            const T mxf = g.mx[f], myf = g.my[f], lxf = g.lx[f], lyf = g.ly[f];
+            // unit tangent p1 -> p2 (readmesh.cpp:400-406) from the normal: mx = dx/|d| = -ny and
+            // my = dy/|d| = nx, bit for bit (same |d| expression, sign-symmetric rounding)
+            const T mxf = -fny, myf = fnx, lxf = g.lx[f], lyf = g.ly[f];
             T dQx[4], dQy[4];
 #pragma unroll
             for (int j = 0; j < 4; j++) {
@@ -318,7 +323,7 @@ __device__ __forceinline__ void face_flux(int f, const DevMesh<T>& m, const Q4<T
 }
 
 template <class T, bool ORDER2, bool NS, bool LAST>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1)
 k_face(int nf, DevMesh<T> m, const Q4<T>* __restrict__ Q, const Q4<T>* __restrict__ G, Q4<T>* __restrict__ tout,
        T* __restrict__ sout, Consts<T> k, int init_prims) {
     const int f = blockIdx.x * blockDim.x + threadIdx.x;

@@ -67,6 +67,7 @@ public:
         size_t o_r = take(q4 * nc_), o_dt = take(sizeof(T) * nc_), o_S = take(sizeof(T) * nc_);
         size_t o_vol = take(sizeof(T) * nc_), o_ixx = take(8 * nc_), o_iyy = take(8 * nc_), o_ixy = take(8 * nc_);
         size_t o_incoff = take(4 * (nc_ + 1)), o_inc = take(4 * (size_t)ninc_), o_nbr = take(4 * (size_t)ninc_);
+        size_t o_igeo = take(q4 * (size_t)ninc_);
         size_t o_fc1 = take(4 * (size_t)nf_), o_fc2 = take(4 * (size_t)nf_), o_qcell = take(4 * (size_t)nf_);
         size_t o_geo[14];
         for (int gI = 0; gI < 14; gI++) o_geo[gI] = gI < ngeo ? take(sizeof(T) * nf_) : 0;
@@ -93,6 +94,7 @@ public:
         g_.mx = geo[9]; g_.my = geo[10]; g_.lx = geo[11]; g_.ly = geo[12]; g_.dist = geo[13];
         t_ = (Q4<T>*)(a + o_t); s_ = (T*)(a + o_s);
         dm_.inc_off = inc_off_; dm_.inc = inc_; dm_.nbr = nbr_; dm_.fc1 = fc1_; dm_.fc2 = fc2_; dm_.qcell = qcell_;
+        dm_.igeo = (const Q4<T>*)(a + o_igeo);
         dm_.g = g_; dm_.Ixx = Ixx_; dm_.Iyy = Iyy_; dm_.Ixy = Ixy_; dm_.vol = vol_;
         smax_ = (T*)(a + o_smax); flag_ = (int*)(a + o_flag);
         n2o_ = (int*)(a + o_n2o); dstage_ = (double*)(a + o_stage); part_ = (double*)(a + o_part);
@@ -129,6 +131,11 @@ public:
         if ((rc = put(Ixy_, L.Ixy.data(), 8 * (size_t)nc_))) return rc;
         if ((rc = putT(vol_, L.vol))) return rc;
         for (int gI = 0; gI < ngeo; gI++) if ((rc = putT(geo[gI], L.fgeo[gI]))) return rc;
+        for (size_t i0 = 0; i0 < L.igeo.size(); i0 += staging_bytes_ / sizeof(T)) {   // staged in chunks
+            const size_t n0 = std::min(L.igeo.size() - i0, staging_bytes_ / sizeof(T));
+            std::vector<double> part(L.igeo.begin() + i0, L.igeo.begin() + i0 + n0);
+            if ((rc = putT((T*)(a + o_igeo) + i0, part))) return rc;
+        }
         return reset_freestream();
     }
 

@@ -31,7 +31,7 @@ EXPORTS = [
     "fv2d_kernel_times", "fv2d_stream", "fv2d_device_bytes", "fv2d_last_error", "fv2d_residual_noalloc",
     "fv2d_batch_create", "fv2d_batch_destroy", "fv2d_batch_footprint", "fv2d_batch_add", "fv2d_batch_remove",
     "fv2d_batch_step", "fv2d_batch_norms", "fv2d_batch_get_state", "fv2d_batch_synchronize", "fv2d_batch_set_tuning",
-    "fv2d_batch_get_tuning", "fv2d_batch_usage", "fv2d_batch_set_kernel_timing", "fv2d_batch_kernel_times",
+    "fv2d_batch_get_tuning", "fv2d_batch_set_grid_mode", "fv2d_batch_usage", "fv2d_batch_set_kernel_timing", "fv2d_batch_kernel_times",
     "fv2d_batch_stream",
 ]
 
@@ -110,6 +110,7 @@ def library():
             "fv2d_batch_synchronize": (ctypes.c_int, [vp]),
             "fv2d_batch_set_tuning": (ctypes.c_int, [vp, ctypes.c_int, ip, ip]),
             "fv2d_batch_get_tuning": (ctypes.c_int, [vp, ip, ip, ip]),
+            "fv2d_batch_set_grid_mode": (ctypes.c_int, [vp, ctypes.c_int]),
             "fv2d_batch_usage": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_longlong)]),
             "fv2d_batch_set_kernel_timing": (ctypes.c_int, [vp, ctypes.c_int]),
             "fv2d_batch_kernel_times": (ctypes.c_int, [vp, dp, ip]),
@@ -368,6 +369,9 @@ class Batch:
         tm = np.asarray(tile_mult, np.int32)
         be = np.asarray(bucket_edges, np.int32)
         _check(library().fv2d_batch_set_tuning(self.h, block, _ip(tm), _ip(be)))
+
+    def set_grid_mode(self, full_grid: bool):
+        _check(library().fv2d_batch_set_grid_mode(self.h, int(full_grid)))
 
     def get_tuning(self):
         b = ctypes.c_int()

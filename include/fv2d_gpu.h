@@ -177,6 +177,9 @@ int fv2d_batch_synchronize(fv2d_batch* b);
  * bucket_edges[0] and bucket_edges[1] cells                                                     */
 int fv2d_batch_set_tuning(fv2d_batch* b, int block, const int* tile_mult3, const int* bucket_edges2);
 int fv2d_batch_get_tuning(fv2d_batch* b, int* block, int* tile_mult3, int* bucket_edges2);
+/* grid of the stage kernels: 0 = persistent (SMs x resident blocks loop over the tiles),
+ * 1 = one block per tile (the graph is re-captured when the tile count changes)                 */
+int fv2d_batch_set_grid_mode(fv2d_batch* b, int full_grid);
 /* cells used/capacity, faces used/capacity, incidences used/capacity, active solves, bytes      */
 int fv2d_batch_usage(fv2d_batch* b, long long* out8);
 int fv2d_batch_set_kernel_timing(fv2d_batch* b, int enable);
