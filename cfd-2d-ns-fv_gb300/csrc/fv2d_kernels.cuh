@@ -52,11 +52,26 @@ __device__ __forceinline__ Q4<T> ldq(const Q4<T>* __restrict__ a, int i) {
     return a[i];
 }
 
+// Ordered comparison a < b.  For doubles it runs on the integer pipe: a non-NaN double's bit
+// pattern, with -0 folded onto +0 and the magnitude bits of negatives inverted, orders exactly as
+// IEEE '<' (equal values, +0 and -0 included, give equal keys), and on GB300 the FP64 pipe, which
+// would otherwise execute DSETP, is 1/32 the width of the integer pipe.  (NaN inputs, which only
+// arise in states already flagged as non-physical, may order differently.)
+__device__ __forceinline__ long long order_key(double x) {
+    long long b = __double_as_longlong(x);
+    b = (b == (long long)0x8000000000000000ULL) ? 0LL : b;
+    return b ^ ((b >> 63) & 0x7FFFFFFFFFFFFFFFLL);
+}
+template <class T>
+__device__ __forceinline__ bool less(T a, T b) { return a < b; }
+template <>
+__device__ __forceinline__ bool less<double>(double a, double b) { return order_key(a) < order_key(b); }
+
 // std::min({a, b}) / std::max({a, b}) semantics (first argument wins ties)
 template <class T>
-__device__ __forceinline__ T min2(T a, T b) { return (b < a) ? b : a; }
+__device__ __forceinline__ T min2(T a, T b) { return less(b, a) ? b : a; }
 template <class T>
-__device__ __forceinline__ T max2(T a, T b) { return (a < b) ? b : a; }
+__device__ __forceinline__ T max2(T a, T b) { return less(a, b) ? b : a; }
 
 // class_Q::updateflow for one state (class_q.hpp:131-141); T (temperature) is never read by the
 // step and is not formed.
@@ -101,11 +116,22 @@ __device__ __forceinline__ void gradient_cell(int c, const DevMesh<T>& m, const 
     if (SQUEEZE)
         for (int j = 0; j < 4; j++) { qmin[j] = T(100000000000.0); qmax[j] = T(-100000000000.0); }
     const int b = inc_off[c], e = inc_off[c + 1];
+    // software-pipelined: the next incidence's record and neighbour state are requested before
+    // the current one is processed (every cell has at least 3 faces, so entry b exists)
+    int inc_n = inc[b], nb_n = nbr[b];
+    Q4<T> ig_n = ldq(m.igeo, b), qn_n;
+    if (nb_n >= 0) qn_n = ldq(Q, nb_n);
     for (int i = b; i < e; i++) {
-        const int f = inc[i] >> 1, side = inc[i] & 1, nb = nbr[i];
+        const int f = inc_n >> 1, side = inc_n & 1, nb = nb_n;
+        const Q4<T> ig = ig_n, qn = qn_n;
+        if (i + 1 < e) {
+            inc_n = inc[i + 1];
+            nb_n = nbr[i + 1];
+            ig_n = ldq(m.igeo, i + 1);
+            if (nb_n >= 0) qn_n = ldq(Q, nb_n);
+        }
         T d[4];
         if (nb >= 0) {
-            const Q4<T> qn = ldq(Q, nb);
             const T* q1 = side == 0 ? qc.p : qn.p;   // reference orientation: c2 - c1
             const T* q2 = side == 0 ? qn.p : qc.p;
 #pragma unroll
@@ -143,7 +169,6 @@ __device__ __forceinline__ void gradient_cell(int c, const DevMesh<T>& m, const 
 #pragma unroll
                 for (int j = 0; j < 4; j++) { qmin[j] = min2(qmin[j], qc.p[j]); qmax[j] = max2(qmax[j], qc.p[j]); }
         }
-        const Q4<T> ig = ldq(m.igeo, i);
         const T fx = ig.p[0], fy = ig.p[1];
 #pragma unroll
         for (int j = 0; j < 4; j++) { sx[j] += d[j] * fx; sy[j] += d[j] * fy; }
@@ -166,8 +191,8 @@ __device__ __forceinline__ void gradient_cell(int c, const DevMesh<T>& m, const 
             for (int j = 0; j < 4; j++) {
                 const T qf = first_stage ? T(-101) : qp.p[j] + gpx.p[j] * dx + gpy.p[j] * dy;
                 T ph = T(1);
-                if (qf < qmin[j]) ph = (qmin[j] - qc.p[j]) / (qf - qc.p[j]);
-                else if (qf > qmax[j]) ph = (qmax[j] - qc.p[j]) / (qf - qc.p[j]);
+                if (less(qf, qmin[j])) ph = (qmin[j] - qc.p[j]) / (qf - qc.p[j]);
+                else if (less(qmax[j], qf)) ph = (qmax[j] - qc.p[j]) / (qf - qc.p[j]);
                 phi[j] = min2(ph, phi[j]);
             }
         }
@@ -181,7 +206,7 @@ __device__ __forceinline__ void gradient_cell(int c, const DevMesh<T>& m, const 
 // Occupancy: the FP32 kernels are latency-bound gathers, so their register use is capped for more
 // resident warps; the FP64 kernels are FP64-ALU-bound and keep their registers.
 template <class T, bool SQUEEZE>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 5 : 1)
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 5 : 2)
 k_gradient(int nc, DevMesh<T> m, const Q4<T>* __restrict__ Q, const Q4<T>* __restrict__ Qprev,
            const Q4<T>* __restrict__ Gprev, Q4<T>* __restrict__ Gout, Consts<T> k, int first_stage, int init_prims) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
