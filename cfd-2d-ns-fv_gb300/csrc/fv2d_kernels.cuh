@@ -84,6 +84,42 @@ __device__ __forceinline__ void prims(const T p[4], const Consts<T>& k, T& rho, 
     P = (E - (T(0.5) * rho * (u * u + v * v))) * k.gm1;
 }
 
+// Division sharing one reciprocal between several quotients with the same denominator.
+// FP64: y = RN(1/b) (__drcp_rn), then two of Markstein's residual corrections
+// (P. Markstein, "Computation of elementary functions on the IBM RISC System/6000 processor",
+// IBM J. Res. Dev. 34(1), 1990): q0 = RN(a*y) is within 1.5 ulp of a/b, the first correction
+// q1 = q0 + RN(a - b*q0)*y brings it within 1 ulp, and with that faithful q1 the residual
+// a - b*q1 is exact and q2 = RN(q1 + (a - b*q1)*y) is the correctly rounded a/b.  Valid for
+// normal operands whose quotient neither overflows nor underflows (all solver quantities); a zero
+// numerator returns the exact signed zero a*y.  Tested bit for bit against IEEE division.
+// FP32 divides directly (the FP32 engine is built with approximate division).
+template <class T>
+struct Recip {
+    static __device__ __forceinline__ T of(T b) { return T(1) / b; }
+    static __device__ __forceinline__ T div(T a, T b, T) { return a / b; }
+};
+template <>
+struct Recip<double> {
+    static __device__ __forceinline__ double of(double b) { return __drcp_rn(b); }
+    static __device__ __forceinline__ double div(double a, double b, double y) {
+        const double q0 = a * y;
+        if (a == 0.0) return q0;
+        const double q1 = __fma_rn(__fma_rn(-b, q0, a), y, q0);
+        return __fma_rn(__fma_rn(-b, q1, a), y, q1);
+    }
+};
+
+// prims() with the reciprocal of rho shared by u, v (and returned for P/rho)
+template <class T>
+__device__ __forceinline__ void prims_r(const T p[4], const Consts<T>& k, T& rho, T& u, T& v, T& P, T& y) {
+    rho = p[0];
+    const T E = p[3];
+    y = Recip<T>::of(rho);
+    u = Recip<T>::div(p[1], rho, y);
+    v = Recip<T>::div(p[2], rho, y);
+    P = (E - (T(0.5) * rho * (u * u + v * v))) * k.gm1;
+}
+
 // class_flow::updateQ (class_flow.hpp:28-34)
 template <class T>
 __device__ __forceinline__ void cons(T rho, T u, T v, T P, const Consts<T>& k, T q[4]) {
@@ -147,10 +183,10 @@ __device__ __forceinline__ void gradient_cell(int c, const DevMesh<T>& m, const 
 #pragma unroll
                 for (int j = 0; j < 4; j++) d[j] = k.q_inf[j] - qc.p[j];
             } else if (nb == -2 || nb == -4) {
-                T rho, u, v, P;
+                T rho, u, v, P, yr;
                 if (init_prims) { rho = k.rho_inf; u = k.u_inf; v = k.v_inf; P = k.P_inf; }
-                else if (nb == -2) prims(qc.p, k, rho, u, v, P);
-                else { const Q4<T> qq = ldq(Q, qcell[f]); prims(qq.p, k, rho, u, v, P); }
+                else if (nb == -2) prims_r(qc.p, k, rho, u, v, P, yr);
+                else { const Q4<T> qq = ldq(Q, qcell[f]); prims_r(qq.p, k, rho, u, v, P, yr); }
                 T gq[4];
                 if (nb == -2) {        // slip wall: reflect the cell velocity (cell_gradient.cpp:43-55)
                     const T fnx = g.nx[f], fny = g.ny[f];
@@ -240,9 +276,9 @@ __device__ __forceinline__ void face_flux(int f, const DevMesh<T>& m, const Q4<T
 #pragma unroll
         for (int j = 0; j < 4; j++) L[j] = q1.p[j] + g1x.p[j] * dx + g1y.p[j] * dy;
     }
-    T lrho, lu, lv, lP;
-    prims(L, k, lrho, lu, lv, lP);
-    const T lc = sqrt(k.gamma * (lP / lrho));
+    T lrho, lu, lv, lP, ly;
+    prims_r(L, k, lrho, lu, lv, lP, ly);
+    const T lc = sqrt(k.gamma * Recip<T>::div(lP, lrho, ly));
     Q4<T> q2, g2x, g2y;
     if (c2 >= 0) {
         q2 = ldq(Q, c2);
@@ -266,9 +302,9 @@ __device__ __forceinline__ void face_flux(int f, const DevMesh<T>& m, const Q4<T
     } else {
         cons(lrho, -lu, -lv, lP, k, Rq);
     }
-    T rrho, ru, rv, rP;
-    prims(Rq, k, rrho, ru, rv, rP);
-    const T rc = sqrt(k.gamma * (rP / rrho));
+    T rrho, ru, rv, rP, ry_;
+    prims_r(Rq, k, rrho, ru, rv, rP, ry_);
+    const T rc = sqrt(k.gamma * Recip<T>::div(rP, rrho, ry_));
 
     // Rusanov
     const T vn1 = lu * fnx + lv * fny;
@@ -288,29 +324,30 @@ __device__ __forceinline__ void face_flux(int f, const DevMesh<T>& m, const Q4<T
         T Aq[4];
 #pragma unroll
         for (int j = 0; j < 4; j++) Aq[j] = T(0.5) * (L[j] + Rq[j]);
-        T arho, au, av, aP;
-        prims(Aq, k, arho, au, av, aP);
+        T arho, au, av, aP, ya;
+        prims_r(Aq, k, arho, au, av, aP, ya);
         T ux = T(0), uy = T(0), vx = T(0), vy = T(0), Px = T(0), Py = T(0), rx = T(0), ry = T(0);
         bool have = true;
         if (c2 >= 0) {
             const T ad = fabs(g.dist[f]);
+            const T yd = Recip<T>::of(ad);
             // unit tangent p1 -> p2 (readmesh.cpp:400-406) from the normal: mx = dx/|d| = -ny and
             // my = dy/|d| = nx, bit for bit (same |d| expression, sign-symmetric rounding)
             const T mxf = -fny, myf = fnx, lxf = g.lx[f], lyf = g.ly[f];
             T dQx[4], dQy[4];
 #pragma unroll
             for (int j = 0; j < 4; j++) {
-                const T dl = (q2.p[j] - q1.p[j]) / ad;
+                const T dl = Recip<T>::div(q2.p[j] - q1.p[j], ad, yd);
                 const T dm = T(0.5) * (g1x.p[j] * mxf + g1y.p[j] * myf + g2x.p[j] * mxf + g2y.p[j] * myf);
                 dQy[j] = dl * lyf + dm * lyf;
                 dQx[j] = dl * lxf + dm * lxf;
             }
             rx = dQx[0];
-            ux = dQx[1] - rx * au / arho;
-            vx = dQx[2] - rx * av / arho;
+            ux = dQx[1] - Recip<T>::div(rx * au, arho, ya);
+            vx = dQx[2] - Recip<T>::div(rx * av, arho, ya);
             ry = dQy[0];
-            uy = dQy[1] - ry * au / arho;
-            vy = dQy[2] - ry * au / arho;          // reconstruction.cpp:155 uses u
+            uy = dQy[1] - Recip<T>::div(ry * au, arho, ya);
+            vy = dQy[2] - Recip<T>::div(ry * au, arho, ya);   // reconstruction.cpp:155 uses u
             Px = k.gm1 * (dQx[3] - T(0.5) * rx * (au * au + av * av) - arho * (au * ux + av * vx));
             Py = k.gm1 * (dQy[3] - T(0.5) * ry * (au * au + av * av) - arho * (au * uy + av * vy));
         } else if (c2 == -4) {
@@ -319,7 +356,8 @@ __device__ __forceinline__ void face_flux(int f, const DevMesh<T>& m, const Q4<T
             T cu, cv;
             if (init_prims) { cu = k.u_inf; cv = k.v_inf; }
             else { cu = q1.p[1] / q1.p[0]; cv = q1.p[2] / q1.p[0]; }
-            const T dudn = -cu / dn, dvdn = -cv / dn;
+            const T ydn = Recip<T>::of(dn);
+            const T dudn = Recip<T>::div(-cu, dn, ydn), dvdn = Recip<T>::div(-cv, dn, ydn);
             ux = dudn * fnx; uy = dudn * fny;
             vx = dvdn * fnx; vy = dvdn * fny;
         } else if (c2 == -2) {
@@ -327,11 +365,13 @@ __device__ __forceinline__ void face_flux(int f, const DevMesh<T>& m, const Q4<T
         }
         T txx, txy, tyy, dTx, dTy;
         if (have) {
-            txx = T(2) * k.mu * (ux - (ux + vy) / T(3));
+            const T third = Recip<T>::div(ux + vy, T(3), T(1.0 / 3.0));
+            txx = T(2) * k.mu * (ux - third);
             txy = k.mu * (uy + vx);
-            tyy = T(2) * k.mu * (vy - (ux + vy) / T(3));
-            dTx = (Px * arho - rx * aP) / (k.R * arho * arho);
-            dTy = (Py * arho - ry * aP) / (k.R * arho * arho);
+            tyy = T(2) * k.mu * (vy - third);
+            const T den = k.R * arho * arho, yden = Recip<T>::of(den);
+            dTx = Recip<T>::div(Px * arho - rx * aP, den, yden);
+            dTy = Recip<T>::div(Py * arho - ry * aP, den, yden);
         } else {
             txx = T(0); txy = T(0); tyy = T(0); dTx = T(0); dTy = T(0);
         }
@@ -442,8 +482,9 @@ __device__ __forceinline__ T update_cell(int c, const DevMesh<T>& m, const Q4<T>
         }
     }
     const T vc = m.vol[c];
+    const T yv = Recip<T>::of(vc);
 #pragma unroll
-    for (int j = 0; j < 4; j++) r[j] = r[j] / vc;
+    for (int j = 0; j < 4; j++) r[j] = Recip<T>::div(r[j], vc, yv);
     if (Rout) { Q4<T> rr; for (int j = 0; j < 4; j++) rr.p[j] = r[j]; Rout[c] = rr; }
     const Q4<T> qn = ldq(Qn, c);
     Q4<T> out;
