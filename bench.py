@@ -325,6 +325,31 @@ def measure_batched(pkg, args, peak, peak_kind):
             "workload": "256 bump-channel Voronoi solves, cells log-uniform 2k-200k, FP32, one graph per iteration"}
 
 
+def measure_serving(pkg, args):
+    """c5 sample: a Poisson stream through continuous batching (FP32) and, as the baseline, the
+    same stream one request at a time through the plain FP64 path, each for `serve_seconds`."""
+    from fv2d_gb300 import serve, workloads
+    t0 = time.time()
+    pool = serve.MeshPool(lo=5e3, hi=2e6, n=args.pool_meshes, seed=args.seed)
+    t_pool = time.time() - t0
+    stream = workloads.c5_stream(rate=args.serve_rate, duration=args.serve_seconds, seed=args.seed, lo=5e3, hi=2e6)
+    budget = args.serve_budget_gb * 1e9
+    cells, faces, solves = serve.capacity_from_budget(pool, budget)
+    b = pkg.Batch(cells, faces, solves, precision=pkg.FP32)
+    b.set_grid_mode(True)
+    out = serve.serve(b, stream, pool, duration=args.serve_seconds, target=1e-6, max_iters=args.serve_max_iters,
+                      check_every=25)
+    usage = b.usage()
+    b.close()
+    base = serve.serve_one_at_a_time(stream, pool, duration=args.serve_seconds, precision=pkg.FP64, target=1e-6,
+                                     max_iters=args.serve_max_iters, check_every=25)
+    return {"batched_fp32": out, "baseline_fp64_one_at_a_time": base,
+            "stream": {"rate_per_s": args.serve_rate, "seconds": args.serve_seconds, "requests": len(stream),
+                       "cells": "log-uniform 5k-2M (snapped to a pool of %d meshes)" % args.pool_meshes},
+            "arena": {"budget_gb": args.serve_budget_gb, "cells": cells, "faces": faces, "bytes": usage["bytes"]},
+            "pool_gen_s": round(t_pool, 1)}
+
+
 def run_partial(args):
     """One measurement alone (profiling runs): --only fp32 | batched."""
     import torch
@@ -332,7 +357,9 @@ def run_partial(args):
     pkg.build.build()
     torch.cuda.set_device(0)
     peak, peak_kind = peaks()
-    if args.only == "fp32":
+    if args.only == "serve":
+        out = measure_serving(pkg, args)
+    elif args.only == "fp32":
         grid, case = make_grid(pkg, args.cells), workload_case(pkg, args.cells)
         N, F = grid.num_cells, grid.num_faces
         Nb = int((grid.fc2 <= 0).sum())
@@ -429,6 +456,10 @@ def run_gpu_arm(args):
         batched = measure_batched(pkg, args, peak, peak_kind)
         batched["vs_fp64_plain"] = round(batched["value"] / value * ws, 2)
 
+    serving = None
+    if rank == 0 and not args.no_serve:
+        serving = measure_serving(pkg, args)
+
     # ---- CPU baseline (oracle port, 1 core, bounded sample)
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -451,7 +482,7 @@ def run_gpu_arm(args):
                 "kernels": {k: {"avg_ms": round(v["avg_ms"], 4), "launches": v["launches"],
                                 "bytes_per_launch": int(v["bytes"]),
                                 "gbs": round(v["bytes"] / (v["avg_ms"] * 1e-3) / 1e9, 1)} for k, v in per.items()},
-                "fp32": fp32, "batched": batched,
+                "fp32": fp32, "batched": batched, "serving": serving,
                 "residual_norm": [float(x) for x in norm], "device_bytes": dev_bytes}
         print(json.dumps(line), flush=True)
     if ws > 1:
@@ -475,7 +506,13 @@ def main():
     ap.add_argument("--batch-solves", type=int, default=256)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-tune", action="store_true")
-    ap.add_argument("--only", default="all", choices=["all", "fp32", "batched"])
+    ap.add_argument("--only", default="all", choices=["all", "fp32", "batched", "serve"])
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-seconds", type=float, default=30.0)
+    ap.add_argument("--serve-rate", type=float, default=50.0)
+    ap.add_argument("--serve-budget-gb", type=float, default=180.0)
+    ap.add_argument("--serve-max-iters", type=int, default=2000)
+    ap.add_argument("--pool-meshes", type=int, default=12)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

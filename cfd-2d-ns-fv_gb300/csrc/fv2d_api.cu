@@ -295,6 +295,14 @@ int fv2d_batch_add(fv2d_batch* b, const fv2d_mesh_desc* desc, const fv2d_case* c
     FV2D_BRET(b, b->b->add(desc, cs, solve_id));
 }
 
+int fv2d_batch_add_mesh(fv2d_batch* b, const fv2d_mesh* mesh, const fv2d_case* cs, int* solve_id) {
+    FV2D_BH(b);
+    if (!mesh || !solve_id) return fail(FV2D_ERR_ARG, "null argument");
+    int rc = check_case(cs);
+    if (rc) return rc;
+    FV2D_BRET(b, b->b->add_mesh(mesh->m, cs, solve_id));
+}
+
 int fv2d_batch_remove(fv2d_batch* b, int solve_id) { FV2D_BH(b); FV2D_BRET(b, b->b->remove(solve_id)); }
 int fv2d_batch_step(fv2d_batch* b, int iterations) { FV2D_BH(b); FV2D_BRET(b, b->b->step(iterations)); }
 

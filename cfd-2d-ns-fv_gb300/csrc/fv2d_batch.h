@@ -23,6 +23,7 @@ public:
     virtual ~Batch() {}
     virtual int init(long long max_cells, long long max_faces, int max_solves) = 0;
     virtual int add(const fv2d_mesh_desc* d, const fv2d_case* cs, int* sid) = 0;
+    virtual int add_mesh(const HostMesh& hm, const fv2d_case* cs, int* sid) = 0;
     virtual int remove(int sid) = 0;
     virtual int step(int iterations) = 0;
     virtual int norms(int* sids, double* out, int* iters, int max, int* n) = 0;

@@ -279,12 +279,18 @@ public:
     }
 
     int add(const fv2d_mesh_desc* d, const fv2d_case* cs, int* sid_out) override {
-        int sid = -1;
-        for (int i = 0; i < S_; i++) if (!recs_[i].active) { sid = i; break; }
-        if (sid < 0) { err_ = "batch is full (max solves)"; return FV2D_ERR_NOMEM; }
         HostMesh hm;
         int rc = build_mesh(d, cs, hm, err_);
         if (rc) return rc;
+        return add_mesh(hm, cs, sid_out);
+    }
+
+    int add_mesh(const HostMesh& hm, const fv2d_case* cs, int* sid_out) override {
+        if (hm.bc1 != cs->bc1 || hm.bc2 != cs->bc2) { err_ = "mesh was built with other BC codes than this case"; return FV2D_ERR_ARG; }
+        int sid = -1;
+        for (int i = 0; i < S_; i++) if (!recs_[i].active) { sid = i; break; }
+        if (sid < 0) { err_ = "batch is full (max solves)"; return FV2D_ERR_NOMEM; }
+        int rc;
         DeviceLayout L;
         build_layout(hm, L);
         Rec r;

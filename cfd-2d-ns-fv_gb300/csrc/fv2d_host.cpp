@@ -367,6 +367,7 @@ int build_mesh(const fv2d_mesh_desc* d, const fv2d_case* cs, HostMesh& m, std::s
     }
     if (d->num_points <= 0 || d->num_faces <= 0 || d->num_cells <= 0) { err = "empty mesh"; return FV2D_ERR_MESH; }
     m.np = d->num_points; m.nf = d->num_faces; m.nc = d->num_cells;
+    m.bc1 = cs->bc1; m.bc2 = cs->bc2;
     m.x.assign(d->x, d->x + m.np);
     m.y.assign(d->y, d->y + m.np);
     int rc = connectivity(d, cs, m, err);

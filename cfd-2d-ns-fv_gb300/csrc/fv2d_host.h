@@ -15,6 +15,7 @@ namespace fv2d {
 struct HostMesh {
     int np = 0, nf = 0, nc = 0;
     int numBC1 = 0, numBC2 = 0, numWALL = -1, num_of_BC = 0, max_sides = 0;
+    int bc1 = 0, bc2 = 0;                    // the BC codes the mesh was tagged with
     std::vector<double> x, y;
     // connectivity, reference numbering (0-based; fc2 < 0 is a BC code)
     std::vector<int> fp1, fp2, fc1, fc2;

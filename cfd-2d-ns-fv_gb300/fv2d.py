@@ -29,7 +29,8 @@ EXPORTS = [
     "fv2d_step", "fv2d_stage", "fv2d_set_state", "fv2d_load_state", "fv2d_get_state", "fv2d_get_field", "fv2d_residual_norm",
     "fv2d_sizes", "fv2d_synchronize", "fv2d_set_store_residual", "fv2d_set_graphs", "fv2d_set_kernel_timing",
     "fv2d_kernel_times", "fv2d_stream", "fv2d_device_bytes", "fv2d_last_error", "fv2d_residual_noalloc",
-    "fv2d_batch_create", "fv2d_batch_destroy", "fv2d_batch_footprint", "fv2d_batch_add", "fv2d_batch_remove",
+    "fv2d_batch_create", "fv2d_batch_destroy", "fv2d_batch_footprint", "fv2d_batch_add", "fv2d_batch_add_mesh",
+    "fv2d_batch_remove",
     "fv2d_batch_step", "fv2d_batch_norms", "fv2d_batch_get_state", "fv2d_batch_synchronize", "fv2d_batch_set_tuning",
     "fv2d_batch_get_tuning", "fv2d_batch_set_grid_mode", "fv2d_batch_usage", "fv2d_batch_set_kernel_timing", "fv2d_batch_kernel_times",
     "fv2d_batch_stream",
@@ -103,6 +104,7 @@ def library():
             "fv2d_batch_destroy": (None, [vp]),
             "fv2d_batch_footprint": (ctypes.c_int, [ctypes.POINTER(MeshDesc), ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)]),
             "fv2d_batch_add": (ctypes.c_int, [vp, ctypes.POINTER(MeshDesc), ctypes.POINTER(Case), ip]),
+            "fv2d_batch_add_mesh": (ctypes.c_int, [vp, vp, ctypes.POINTER(Case), ip]),
             "fv2d_batch_remove": (ctypes.c_int, [vp, ctypes.c_int]),
             "fv2d_batch_step": (ctypes.c_int, [vp, ctypes.c_int]),
             "fv2d_batch_norms": (ctypes.c_int, [vp, ip, dp, ip, ctypes.c_int, ip]),
@@ -338,6 +340,15 @@ class Batch:
         sid = ctypes.c_int()
         _check(library().fv2d_batch_add(self.h, ctypes.byref(d.desc), ctypes.byref(case), ctypes.byref(sid)))
         self.cells[sid.value] = grid.num_cells
+        return sid.value
+
+    def add_mesh(self, host_mesh, case) -> int:
+        """Admit a solve on a prebuilt HostMesh (built with the same BC codes as `case`)."""
+        if isinstance(case, dict):
+            case = case_from_dict(case)
+        sid = ctypes.c_int()
+        _check(library().fv2d_batch_add_mesh(self.h, host_mesh.h, ctypes.byref(case), ctypes.byref(sid)))
+        self.cells[sid.value] = host_mesh.nc
         return sid.value
 
     def remove(self, sid: int):

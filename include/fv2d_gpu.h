@@ -167,6 +167,9 @@ void fv2d_batch_destroy(fv2d_batch* b);
 int fv2d_batch_footprint(const fv2d_mesh_desc* desc, int precision, long long* bytes);
 /* FV2D_ERR_NOMEM when the arena has no room (the batch is unchanged)                           */
 int fv2d_batch_add(fv2d_batch* b, const fv2d_mesh_desc* desc, const fv2d_case* cs, int* solve_id);
+/* the same from a host mesh built by fv2d_mesh_build with the same BC codes (lets a caller build
+ * meshes ahead of admission, or reuse one for solves that differ only in flow conditions)      */
+int fv2d_batch_add_mesh(fv2d_batch* b, const fv2d_mesh* mesh, const fv2d_case* cs, int* solve_id);
 int fv2d_batch_remove(fv2d_batch* b, int solve_id);
 int fv2d_batch_step(fv2d_batch* b, int iterations);
 /* for every active solve: id, the 4 residual L2 norms of its last iteration, iterations done   */
