@@ -331,6 +331,7 @@ def measure_serving(pkg, args):
     from fv2d_gb300 import serve, workloads
     t0 = time.time()
     pool = serve.MeshPool(lo=5e3, hi=2e6, n=args.pool_meshes, seed=args.seed)
+    pool.prebuild()
     t_pool = time.time() - t0
     stream = workloads.c5_stream(rate=args.serve_rate, duration=args.serve_seconds, seed=args.seed, lo=5e3, hi=2e6)
     budget = args.serve_budget_gb * 1e9
@@ -346,7 +347,8 @@ def measure_serving(pkg, args):
     return {"batched_fp32": out, "baseline_fp64_one_at_a_time": base,
             "stream": {"rate_per_s": args.serve_rate, "seconds": args.serve_seconds, "requests": len(stream),
                        "cells": "log-uniform 5k-2M (snapped to a pool of %d meshes)" % args.pool_meshes},
-            "arena": {"budget_gb": args.serve_budget_gb, "cells": cells, "faces": faces, "bytes": usage["bytes"]},
+            "arena": {"budget_gb": args.serve_budget_gb, "cells": cells, "faces": faces, "bytes": usage["bytes"],
+                      "capped_by_32bit_face_ids": faces >= serve.MAX_ARENA_FACES},
             "pool_gen_s": round(t_pool, 1)}
 
 
@@ -510,7 +512,7 @@ def main():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=30.0)
     ap.add_argument("--serve-rate", type=float, default=50.0)
-    ap.add_argument("--serve-budget-gb", type=float, default=180.0)
+    ap.add_argument("--serve-budget-gb", type=float, default=8.0)
     ap.add_argument("--serve-max-iters", type=int, default=2000)
     ap.add_argument("--pool-meshes", type=int, default=12)
     args = ap.parse_args()

@@ -54,6 +54,13 @@ class MeshPool:
         self.cells = np.array([g.num_cells for g in grids], dtype=np.float64)
         self._cache = {}
 
+    def prebuild(self):
+        """Build every host mesh the workload's two boundary-code pairs need (before serving)."""
+        for ns in (False, True):
+            case = workloads.spec_case(dict(mach=0.5, angle=0.0, ns=ns, re=5e3))
+            for i in range(len(self.grids)):
+                self.host_mesh(i, case)
+
     def index_for(self, cells):
         return int(np.argmin(np.abs(np.log(self.cells) - math.log(cells))))
 
@@ -215,10 +222,13 @@ def serve_one_at_a_time(stream, pool, duration, precision=fv2d.FP64, target=1e-6
                 target=target, max_iters=max_iters, check_every=check_every)
 
 
+MAX_ARENA_FACES = (1 << 29) - (1 << 20)    # face ids are 32-bit (face << 1 | side) in the arena
+
+
 def capacity_from_budget(pool, budget_bytes, precision=fv2d.FP32):
     """Batch capacity (cells, faces, solves) whose arena fits in `budget_bytes`, in the proportion
-    of faces to cells of the pool's meshes."""
+    of faces to cells of the pool's meshes, capped by the arena's 32-bit face ids."""
     per_cell = np.mean([fv2d.Batch.footprint(g, precision) / g.num_cells for g in pool.grids])
     faces_per_cell = float(np.mean([g.num_faces / g.num_cells for g in pool.grids]))
-    cells = int(budget_bytes / per_cell)
+    cells = int(min(budget_bytes / per_cell, MAX_ARENA_FACES / faces_per_cell))
     return cells, int(cells * faces_per_cell) + 1024, max(16, min(8192, int(cells / 4000)))
