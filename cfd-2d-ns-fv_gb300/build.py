@@ -38,6 +38,7 @@ def _units():
     return [
         # (source, object, command prefix)
         ("fv2d_host.cpp", host),
+        ("fv2d_output.cpp", host),
         ("fv2d_api.cu", [nvcc] + common),
         # the FP64 engine must not contract a*b+c: bit-identical with the reference
         ("fv2d_fp64.cu", [nvcc] + common + ["-fmad=false"]),

@@ -2,12 +2,14 @@
 #include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <vector>
 #include <string>
 
 #include <cuda_runtime.h>
 
 #include "fv2d_gpu.h"
 #include "fv2d_host.h"
+#include "fv2d_output.h"
 #include "fv2d_batch.h"
 #include "fv2d_solver.h"
 
@@ -19,6 +21,7 @@ const char* const kKernelNames[K_COUNT] = {"k_gradient", "k_face", "k_update", "
 struct fv2d_handle {
     std::unique_ptr<fv2d::Solver> s;
     int precision = FV2D_FP64;
+    fv2d_case cs{};
 };
 
 struct fv2d_mesh {
@@ -157,6 +160,7 @@ int fv2d_create(const fv2d_mesh_desc* desc, const fv2d_case* cs, int precision, 
     if (rc) return fail(rc, err);
     rc = h->s->init(*cs);
     if (rc) return fail(rc, h->s->err_);
+    h->cs = *cs;
     *out = h.release();
     return FV2D_OK;
 }
@@ -222,6 +226,52 @@ int fv2d_sizes(fv2d_handle* h, int* o) {
     o[0] = m.np; o[1] = m.nf; o[2] = m.nc; o[3] = m.numBC1; o[4] = m.numBC2; o[5] = m.numWALL;
     o[6] = m.num_of_BC; o[7] = h->s->current_stage();
     return FV2D_OK;
+}
+
+int fv2d_save(fv2d_handle* h, int ndx) {
+    FV2D_H(h);
+    const int N = h->s->mesh_.nc;
+    std::vector<double> q(4 * (size_t)N), g(8 * (size_t)N), r(4 * (size_t)N);
+    int rc = h->s->get_field(FV2D_F_QBAR, q.data());
+    if (!rc) rc = h->s->get_field(FV2D_F_QBAR_GRAD, g.data());
+    if (!rc) rc = h->s->get_field(FV2D_F_RES, r.data());
+    if (rc && rc != FV2D_ERR_STATE) return fail(rc, h->s->err_);
+    std::string err;
+    int wrc = fv2d::save_solution(h->s->mesh_, h->cs, ndx, q.data(), g.data(), r.data(), "sol", err);
+    if (wrc) return fail(wrc, err);
+    return rc;
+}
+
+int fv2d_post(fv2d_handle* h, int ndx) {
+    FV2D_H(h);
+    std::vector<double> q(4 * (size_t)h->s->mesh_.nc);
+    int rc = h->s->get_field(FV2D_F_QBAR, q.data());
+    if (rc && rc != FV2D_ERR_STATE) return fail(rc, h->s->err_);
+    std::string err;
+    int wrc = fv2d::write_restart(h->s->mesh_, ndx, q.data(), "sol", err);
+    if (wrc) return fail(wrc, err);
+    return rc;
+}
+
+int fv2d_write_history_headers(fv2d_handle* h) {
+    FV2D_H(h);
+    std::string err;
+    int rc = fv2d::write_history_headers("sol", err);
+    return rc ? fail(rc, err) : FV2D_OK;
+}
+
+int fv2d_write_mesh_files(fv2d_handle* h) {
+    FV2D_H(h);
+    std::string err;
+    int rc = fv2d::write_mesh_files(h->s->mesh_, "mesh", err);
+    return rc ? fail(rc, err) : FV2D_OK;
+}
+
+int fv2d_read_restart(const char* path, int num_cells, int* ndx, double* q) {
+    if (!path || !ndx || !q || num_cells <= 0) return fail(FV2D_ERR_ARG, "bad argument");
+    std::string err;
+    int rc = fv2d::read_restart(path, num_cells, ndx, q, err);
+    return rc ? fail(rc, err) : FV2D_OK;
 }
 
 int fv2d_synchronize(fv2d_handle* h) { FV2D_H(h); FV2D_RET(h, h->s->synchronize()); }

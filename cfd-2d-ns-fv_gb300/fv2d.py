@@ -27,7 +27,8 @@ EXPORTS = [
     "fv2d_read_inputs", "fv2d_read_grid", "fv2d_free", "fv2d_mesh_build", "fv2d_mesh_free", "fv2d_mesh_sizes",
     "fv2d_mesh_get", "fv2d_mesh_permutation", "fv2d_create", "fv2d_create_from_files", "fv2d_destroy",
     "fv2d_step", "fv2d_stage", "fv2d_set_state", "fv2d_load_state", "fv2d_get_state", "fv2d_get_field", "fv2d_residual_norm",
-    "fv2d_sizes", "fv2d_synchronize", "fv2d_set_store_residual", "fv2d_set_graphs", "fv2d_set_kernel_timing",
+    "fv2d_sizes", "fv2d_save", "fv2d_post", "fv2d_write_history_headers", "fv2d_write_mesh_files",
+    "fv2d_read_restart", "fv2d_synchronize", "fv2d_set_store_residual", "fv2d_set_graphs", "fv2d_set_kernel_timing",
     "fv2d_kernel_times", "fv2d_stream", "fv2d_device_bytes", "fv2d_last_error", "fv2d_residual_noalloc",
     "fv2d_batch_create", "fv2d_batch_destroy", "fv2d_batch_footprint", "fv2d_batch_add", "fv2d_batch_add_mesh",
     "fv2d_batch_remove",
@@ -92,6 +93,11 @@ def library():
             "fv2d_get_field": (ctypes.c_int, [vp, ctypes.c_int, dp]),
             "fv2d_residual_norm": (ctypes.c_int, [vp, dp]),
             "fv2d_sizes": (ctypes.c_int, [vp, ip]),
+            "fv2d_save": (ctypes.c_int, [vp, ctypes.c_int]),
+            "fv2d_post": (ctypes.c_int, [vp, ctypes.c_int]),
+            "fv2d_write_history_headers": (ctypes.c_int, [vp]),
+            "fv2d_write_mesh_files": (ctypes.c_int, [vp]),
+            "fv2d_read_restart": (ctypes.c_int, [cp, ctypes.c_int, ip, dp]),
             "fv2d_synchronize": (ctypes.c_int, [vp]),
             "fv2d_set_store_residual": (ctypes.c_int, [vp, ctypes.c_int]),
             "fv2d_set_graphs": (ctypes.c_int, [vp, ctypes.c_int]),
@@ -144,6 +150,14 @@ def read_inputs(path: str) -> Case:
     cs = Case()
     _check(library().fv2d_read_inputs(path.encode(), ctypes.byref(cs)))
     return cs
+
+
+def read_restart(path: str, num_cells: int):
+    """(iteration, q[4, num_cells]) from a restart_sol.dat-format file."""
+    q = np.zeros(4 * num_cells, np.float64)
+    ndx = ctypes.c_int()
+    _check(library().fv2d_read_restart(path.encode(), int(num_cells), ctypes.byref(ndx), _dp(q)))
+    return ndx.value, q.reshape(4, num_cells)
 
 
 def case_from_dict(c: dict) -> Case:
@@ -282,6 +296,21 @@ class Solver:
         out = np.zeros(4, np.float64)
         _check(library().fv2d_residual_norm(self.h, _dp(out)), self.h)
         return out
+
+    def save(self, ndx: int):
+        """Monitor / Tecplot output of iteration `ndx` under ./sol (the reference's save())."""
+        _check(library().fv2d_save(self.h, int(ndx)), self.h)
+
+    def post(self, ndx: int):
+        """./sol/restart_sol.dat for iteration `ndx` (the reference's post())."""
+        _check(library().fv2d_post(self.h, int(ndx)), self.h)
+
+    def write_history_headers(self):
+        _check(library().fv2d_write_history_headers(self.h), self.h)
+
+    def write_mesh_files(self):
+        """./mesh/cell_data.dat and ./mesh/face_data.dat."""
+        _check(library().fv2d_write_mesh_files(self.h), self.h)
 
     def set_store_residual(self, every: bool):
         _check(library().fv2d_set_store_residual(self.h, int(every)), self.h)

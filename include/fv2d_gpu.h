@@ -136,6 +136,21 @@ int fv2d_get_field(fv2d_handle* h, int field, double* out);
 int fv2d_residual_norm(fv2d_handle* h, double out4[4]);
 /* sizes: num_points, num_faces, num_cells, numBC1, numBC2, numWALL, num_of_BC, stage          */
 int fv2d_sizes(fv2d_handle* h, int* out8);
+
+/* ---- solution files (the reference's layout, written in the working directory's sol/ and mesh/) */
+/* Monitor line (stdout) + sol/output.dat + sol/res_history.dat every monitor_step, and the
+ * node-averaged Tecplot volume/surface files every output_step, for iteration `ndx`.  Replaces
+ * save() (src/base/save_sol.cpp:16); call it after the iteration's fv2d_step.                  */
+int fv2d_save(fv2d_handle* h, int ndx);
+/* sol/restart_sol.dat for iteration `ndx`.  Replaces post() (src/base/post_process.cpp:13).   */
+int fv2d_post(fv2d_handle* h, int ndx);
+/* Headers of sol/res_history.dat and sol/output.dat (src/base/main.cpp:59-73).                */
+int fv2d_write_history_headers(fv2d_handle* h);
+/* mesh/cell_data.dat and mesh/face_data.dat (src/base/readmesh.cpp:413-446).                  */
+int fv2d_write_mesh_files(fv2d_handle* h);
+/* Read sol/restart_sol.dat-format file into q (4N SoA); *ndx = the iteration it was written at
+ * (src/base/main.cpp:82-104).  Host only.                                                      */
+int fv2d_read_restart(const char* path, int num_cells, int* ndx, double* q);
 int fv2d_synchronize(fv2d_handle* h);
 /* Store the residual after every stage (parity checks) instead of only after the last stage.  */
 int fv2d_set_store_residual(fv2d_handle* h, int every_stage);
