@@ -2,7 +2,10 @@
 sol/res_history.dat, sol/tec_sol*.dat, sol/tec_surf*.dat, sol/restart_sol.dat) against the files the
 REFERENCE program wrote on the same cases (tests/golden/cli/*.npz, made by make_cli_golden.py).
 
-CPU: the library's host writers driven by the oracle port (tests/cpu_helpers/cli_oracle.cpp).
+CPU: the library's host writers driven by the oracle port (tests/cpu_helpers/cli_oracle.cpp); and the
+     reference's own src/base/main.cpp linked with the reference-signature shim
+     (shim/ssp_rk3_gpu.cpp) over the oracle-backed ABI stub (oracle/abi_oracle_stub.cpp), built by
+     `make -C oracle shim` where the reference tree exists.
 GPU: the shipped command-line driver lib/fv2d_gpu (FP64), whose state comes from the GPU engine.
 Both must reproduce every byte but the undefined last-row tau fields of tec_surf (cli_check.masked).
 """
@@ -51,9 +54,30 @@ def test_writers_match_reference_files(oracle_cli, case, tmp_path):
     assert cli_check.run_case([oracle_cli], case, str(tmp_path)) == []
 
 
+@pytest.fixture(scope="module")
+def shim_program():
+    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "shim"], check=True, capture_output=True)
+    prog = os.path.join(ROOT, "oracle", "_ref", "fv2d_ref_shim_oracle")
+    if not os.path.exists(prog):
+        pytest.skip("reference tree not present: the reference main cannot be built here")
+    return prog
+
+
+@pytest.mark.parametrize("case", CASES, ids=lambda p: os.path.basename(p)[:-4])
+def test_reference_main_through_shim(shim_program, case, tmp_path):
+    assert cli_check.run_case([shim_program], case, str(tmp_path)) == []
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("case", CASES, ids=lambda p: os.path.basename(p)[:-4])
 def test_gpu_cli_matches_reference_files(pkg, case, tmp_path):
     prog = pkg.build.CLI
     assert os.path.exists(prog), "lib/fv2d_gpu not built"
     assert cli_check.run_case([prog], case, str(tmp_path)) == []
+
+
+def test_reference_main_links_against_gpu_library(pkg, shim_program):
+    """The link-time swap: the reference's main.cpp + shim resolve every symbol in libfv2d_gb300.so."""
+    assert os.path.exists(pkg.build.LIB)
+    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "shim"], check=True, capture_output=True)
+    assert os.path.exists(os.path.join(ROOT, "oracle", "_ref", "fv2d_ref_shim_gpu"))
