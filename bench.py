@@ -175,6 +175,33 @@ def ncu_traffic(precision, kernel, N, F):
         return None
 
 
+def fp64_pipe(kernels, N, F, sm_mhz):
+    """FP64 path: each kernel's FP64 thread-instructions per launch (per-unit count from the
+    committed ncu capture x this mesh's units) over its live event-timed launch time, against the
+    FP64 issue peak of 2 thread-instructions per SM per cycle at the sampled SM clock."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as fh:
+            t = json.load(fh)["fp64"]
+        import torch
+        sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    except Exception:
+        return None
+    peak = 2.0 * sms * sm_mhz * 1e6 / 1e9
+    out = {}
+    for k, v in kernels.items():
+        if k not in t or "fp64_inst" not in t[k]:
+            continue
+        inst = t[k]["fp64_inst"] / t[k]["units"] * (N if t[k]["per"] == "cells" else F)
+        ach = inst / (v["avg_ms"] * 1e-3) / 1e9
+        out[k] = {"achieved": round(ach, 1), "frac": round(ach / peak, 3), "inst_per_launch": int(inst)}
+    if not out:
+        return None
+    dom = max(kernels, key=lambda k: kernels[k]["total_ms"])
+    return {"bound": "fp64_pipe", "kernel": dom, "achieved": out[dom]["achieved"], "peak": round(peak, 1),
+            "unit": "G FP64 thread-inst/s", "frac": out[dom]["frac"], "sm_mhz": sm_mhz,
+            "per_kernel": out}
+
+
 def peaks():
     try:
         with open(PEAKS_FILE) as fh:
@@ -192,8 +219,29 @@ def cpu_baseline(pkg, orc, grid, case, iters):
     return 3.0 * N * iters / t, t
 
 
+def max_over_ranks(x: float, ws: int) -> float:
+    """The slowest rank's value (MAX all-reduce over the host process group; identity at N=1)."""
+    if ws <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+REF_SAMPLE_S = 40.0           # bounded CPU sample per replica (seconds of work, estimated)
+REF_CELL_STAGE_PER_S = 1.5e6  # conservative single-core rate of the oracle port, for sizing the sample
+
+
+def reference_iterations(steps: int, cells: int) -> int:
+    """Iterations each CPU replica times: `steps`, capped to about REF_SAMPLE_S of work."""
+    return max(1, min(steps, int(REF_SAMPLE_S * REF_CELL_STAGE_PER_S / (3.0 * cells))))
+
+
 def run_reference_arm(args):
-    """Oracle port on the host cores: one replica per core, same mesh and options."""
+    """Oracle port on the host cores: one replica per core, same mesh and options, each timing a
+    bounded sample of iterations (reference_iterations)."""
     import multiprocessing as mp
 
     ws, rank, _ = dist_env()
@@ -208,10 +256,12 @@ def run_reference_arm(args):
     ctx = mp.get_context("fork")       # no CUDA in this process
     q = ctx.Queue()
 
+    iters = reference_iterations(args.steps, grid.num_cells)
+
     def worker(i):
         o = orc.Oracle("port", grid=grid, case=case)
-        o.iterate(max(args.warmup, 1))
-        t = o.time_iterations(args.steps)
+        o.iterate(1)                       # warm-up (allocation, first touch)
+        t = o.time_iterations(iters)
         q.put(t)
 
     t0 = time.time()
@@ -223,16 +273,16 @@ def run_reference_arm(args):
         p.join()
     wall = time.time() - t0
     N = grid.num_cells
-    per_core = [3.0 * N * args.steps / t for t in ts]
+    per_core = [3.0 * N * iters / t for t in ts]
     value = sum(per_core)
     line = {"metric": METRIC, "value": value, "unit": "cell-stage/s", "impl": "reference", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * max(ts) / args.steps,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * max(ts) / iters,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": "ns_cylinder_voronoi", "cells": N, "faces": grid.num_faces, "precision": "fp64",
                        "parallelism": f"{cores} independent CPU replicas"},
             "cpu_baseline": {"value": value, "unit": "cell-stage/s", "cores": cores, "kind": "port",
-                             "sample": f"{args.steps} SSP-RK3 iterations of the {N}-cell solve per core, "
-                                       f"after {max(args.warmup, 1)} warm-up iterations",
+                             "sample": f"{iters} SSP-RK3 iterations of the {N}-cell solve per core "
+                                       f"(of {args.steps} steps, capped to ~{REF_SAMPLE_S:.0f} s), after 1 warm-up",
                              "single_core_value": statistics.median(per_core)},
             "e2e": {"value": value, "unit": "cell-stage/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "wall_s": round(wall, 1)}
@@ -416,11 +466,7 @@ def run_gpu_arm(args):
     ms = e0.elapsed_time(e1)
     clk = clocks.stop()
     barrier()
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, ws)
     value = ws * 3.0 * N * args.steps / (ms * 1e-3)
 
     # ---- per-kernel timing pass (events around every launch, eager launches)
@@ -432,6 +478,8 @@ def run_gpu_arm(args):
     dom, roof, per = roofline(kt, single_kernel_bytes(N, F, ninc, Nb, s_bytes, prec == pkg.FP32), peak)
     roof["peak_source"] = f"{peak_kind} hbm_gbs"
     roof["traffic"] = ncu_traffic(args.precision, dom, N, F)
+    if prec == pkg.FP64:   # this path is bound by the FP64 pipe, not HBM
+        roof["fp64_pipe"] = fp64_pipe(per, N, F, clk.get("sm_mhz") or clk.get("sm_max_mhz") or 2070.0)
     gpu_launches = 3 * 3 * args.steps
 
     # ---- end to end through the C ABI with host buffers: upload Qbar, one iteration, download
@@ -444,7 +492,7 @@ def run_gpu_arm(args):
         solver.step(1)
         solver.get_state(q)
         norm = solver.residual_norm()
-    t_e2e = time.perf_counter() - t0
+    t_e2e = max_over_ranks(time.perf_counter() - t0, ws)
     e2e = {"value": ws * 3.0 * N * args.steps / t_e2e, "unit": "cell-stage/s",
            "h2d_bytes_per_step": 4 * 8 * N, "d2h_bytes_per_step": 4 * 8 * N + 4 * 8}
     dev_bytes = solver.device_bytes()

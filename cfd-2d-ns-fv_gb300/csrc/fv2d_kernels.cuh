@@ -240,9 +240,22 @@ __device__ __forceinline__ void gradient_cell(int c, const DevMesh<T>& m, const 
 }
 
 // Occupancy: the FP32 kernels are latency-bound gathers, so their register use is capped for more
-// resident warps; the FP64 kernels are FP64-ALU-bound and keep their registers.
+// resident warps.  The FP64 kernels are FP64-pipe-bound; their block size and minimum resident
+// blocks (register cap) set how many warps cover the pipe's latency.
+#ifndef FV2D_FP64_BLOCK
+#define FV2D_FP64_BLOCK 256
+#endif
+#ifndef FV2D_FP64_GMINB
+#define FV2D_FP64_GMINB 2
+#endif
+#ifndef FV2D_FP64_FMINB
+#define FV2D_FP64_FMINB 1
+#endif
+template <class T>
+constexpr int kStageBlock = sizeof(T) == 4 ? 256 : FV2D_FP64_BLOCK;   // gradient and face kernels
+
 template <class T, bool SQUEEZE>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 5 : 2)
+__global__ void __launch_bounds__(kStageBlock<T>, sizeof(T) == 4 ? 5 : FV2D_FP64_GMINB)
 k_gradient(int nc, DevMesh<T> m, const Q4<T>* __restrict__ Q, const Q4<T>* __restrict__ Qprev,
            const Q4<T>* __restrict__ Gprev, Q4<T>* __restrict__ Gout, Consts<T> k, int first_stage, int init_prims) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -388,7 +401,7 @@ __device__ __forceinline__ void face_flux(int f, const DevMesh<T>& m, const Q4<T
 }
 
 template <class T, bool ORDER2, bool NS, bool LAST>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1)
+__global__ void __launch_bounds__(kStageBlock<T>, sizeof(T) == 4 ? 4 : FV2D_FP64_FMINB)
 k_face(int nf, DevMesh<T> m, const Q4<T>* __restrict__ Q, const Q4<T>* __restrict__ G, Q4<T>* __restrict__ tout,
        T* __restrict__ sout, Consts<T> k, int init_prims) {
     const int f = blockIdx.x * blockDim.x + threadIdx.x;

@@ -186,16 +186,17 @@ public:
         Q4<T>* qin = Q_[s];
         const int p = (s + 2) % 3;
         if (order2_) {
+            constexpr int B = kStageBlock<T>;
             launch(K_GRADIENT, nc_, [&](int gr) {
                 if (squeeze_)
-                    k_gradient<T, true><<<gr, 256, 0, stream_>>>(nc_, dm_, qin, Q_[p], G_[p], G_[s], k_, fresh_ ? 1 : 0,
-                                                                init_prims_ ? 1 : 0);
+                    k_gradient<T, true><<<gr, B, 0, stream_>>>(nc_, dm_, qin, Q_[p], G_[p], G_[s], k_, fresh_ ? 1 : 0,
+                                                              init_prims_ ? 1 : 0);
                 else
-                    k_gradient<T, false><<<gr, 256, 0, stream_>>>(nc_, dm_, qin, Q_[p], G_[p], G_[s], k_, fresh_ ? 1 : 0,
-                                                                 init_prims_ ? 1 : 0);
-            });
+                    k_gradient<T, false><<<gr, B, 0, stream_>>>(nc_, dm_, qin, Q_[p], G_[p], G_[s], k_, fresh_ ? 1 : 0,
+                                                               init_prims_ ? 1 : 0);
+            }, B);
         }
-        launch(K_FACE, nf_, [&](int gr) { launch_face(gr, qin, G_[s], s == 2); });
+        launch(K_FACE, nf_, [&](int gr) { launch_face(gr, qin, G_[s], s == 2); }, kStageBlock<T>);
         if (s == 2) FV2D_CUDA(cudaMemsetAsync(smax_, 0, sizeof(T), stream_));
         Q4<T>* rout = (store_every_ || s == 2) ? R_ : nullptr;
         launch(K_UPDATE, nc_, [&](int gr) {
@@ -337,7 +338,8 @@ public:
 
 private:
     void launch_face(int gr, const Q4<T>* qin, const Q4<T>* G, bool last) {
-#define FV2D_FACE(O2, NS, LAST) k_face<T, O2, NS, LAST><<<gr, 256, 0, stream_>>>(nf_, dm_, qin, G, t_, s_, k_, init_prims_ ? 1 : 0)
+#define FV2D_FACE(O2, NS, LAST) \
+    k_face<T, O2, NS, LAST><<<gr, kStageBlock<T>, 0, stream_>>>(nf_, dm_, qin, G, t_, s_, k_, init_prims_ ? 1 : 0)
         if (order2_) {
             if (ns_) { if (last) FV2D_FACE(true, true, true); else FV2D_FACE(true, true, false); }
             else { if (last) FV2D_FACE(true, false, true); else FV2D_FACE(true, false, false); }
@@ -348,8 +350,8 @@ private:
     }
 
     template <class F>
-    void launch(int kid, int n, F&& fn) {
-        const int gr = (n + 255) / 256;
+    void launch(int kid, int n, F&& fn, int block = 256) {
+        const int gr = (n + block - 1) / block;
         if (!timing_) { fn(gr > 0 ? gr : 1); return; }
         Pending p;
         p.kid = kid;
