@@ -363,6 +363,7 @@ def measure_batched(pkg, args, peak, peak_kind):
                                           comp=True, store_r=False)
     dom, roof, per = roofline(kt, kbytes, peak)
     roof["peak_source"] = f"{peak_kind} hbm_gbs"
+    roof["traffic"] = ncu_traffic("batch_fp32", dom, tot_c, tot_f)
     norms = b.norms()
     finite = all(np.all(np.isfinite(v[0])) for v in norms.values())
     b.close()
@@ -402,8 +403,27 @@ def measure_serving(pkg, args):
             "pool_gen_s": round(t_pool, 1)}
 
 
+def measure_precision(pkg, args):
+    """c3: FP32 against FP64 (bit-exact) on the 4M-cell Euler bump channel (Mach drawn from the seed,
+    squeeze, LOCAL dt), run to a 1e-6 residual drop or an iteration cap: second order with the
+    squeeze limiter (which stalls near a 5 % drop, so it runs to the cap) and first order (which
+    converges).  Density / pressure L2 and Linf differences and the wall-force difference."""
+    from fv2d_gb300 import precision, workloads
+    t0 = time.time()
+    grid, case, mach = workloads.c3_case(cells=args.prec_cells, seed=args.seed)
+    t_mesh = time.time() - t0
+    out = {"workload": "c3 bump channel, Euler", "cells": grid.num_cells, "faces": grid.num_faces,
+           "mach": round(mach, 4), "seed": args.seed, "mesh_gen_s": round(t_mesh, 1)}
+    out["second_order_squeeze"] = precision.compare(grid, case, drop=1e-6, max_iters=args.prec_max_iters,
+                                                    check_every=100)
+    first = dict(case, solution_poly_order=0, limiter="NONE")
+    out["first_order"] = precision.compare(grid, first, drop=1e-6, max_iters=args.prec_max_iters_first,
+                                           check_every=200)
+    return out
+
+
 def run_partial(args):
-    """One measurement alone (profiling runs): --only fp32 | batched."""
+    """One measurement alone: --only fp32 | batched | serve | precision."""
     import torch
     pkg = entry.load_package()
     pkg.build.build()
@@ -411,6 +431,8 @@ def run_partial(args):
     peak, peak_kind = peaks()
     if args.only == "serve":
         out = measure_serving(pkg, args)
+    elif args.only == "precision":
+        out = measure_precision(pkg, args)
     elif args.only == "fp32":
         grid, case = make_grid(pkg, args.cells), workload_case(pkg, args.cells)
         N, F = grid.num_cells, grid.num_faces
@@ -483,7 +505,9 @@ def run_gpu_arm(args):
     gpu_launches = 3 * 3 * args.steps
 
     # ---- end to end through the C ABI with host buffers: upload Qbar, one iteration, download
-    q = solver.get_state()
+    # the step's input and output live in page-locked host memory (the library DMAs them directly)
+    q = torch.empty(4 * N, dtype=torch.float64, pin_memory=True).numpy()
+    solver.get_state(q)
     norm = np.zeros(4)
     barrier()
     t0 = time.perf_counter()
@@ -493,8 +517,19 @@ def run_gpu_arm(args):
         solver.get_state(q)
         norm = solver.residual_norm()
     t_e2e = max_over_ranks(time.perf_counter() - t0, ws)
+    # the same with ordinary (pageable) host arrays: staged through the library's pinned buffer
+    qp = np.array(q)
+    kp = max(3, min(args.steps, 20))
+    t0 = time.perf_counter()
+    for _ in range(kp):
+        solver.load_state(qp)
+        solver.step(1)
+        solver.get_state(qp)
+        norm = solver.residual_norm()
+    t_pg = max_over_ranks(time.perf_counter() - t0, ws)
     e2e = {"value": ws * 3.0 * N * args.steps / t_e2e, "unit": "cell-stage/s",
-           "h2d_bytes_per_step": 4 * 8 * N, "d2h_bytes_per_step": 4 * 8 * N + 4 * 8}
+           "h2d_bytes_per_step": 4 * 8 * N, "d2h_bytes_per_step": 4 * 8 * N + 4 * 8, "host_buffers": "pinned",
+           "pageable_value": ws * 3.0 * N * kp / t_pg}
     dev_bytes = solver.device_bytes()
     solver.close()
 
@@ -556,7 +591,10 @@ def main():
     ap.add_argument("--batch-solves", type=int, default=256)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-tune", action="store_true")
-    ap.add_argument("--only", default="all", choices=["all", "fp32", "batched", "serve"])
+    ap.add_argument("--only", default="all", choices=["all", "fp32", "batched", "serve", "precision"])
+    ap.add_argument("--prec-cells", type=int, default=4_000_000)
+    ap.add_argument("--prec-max-iters", type=int, default=4000)
+    ap.add_argument("--prec-max-iters-first", type=int, default=20000)
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=30.0)
     ap.add_argument("--serve-rate", type=float, default=50.0)

@@ -62,8 +62,16 @@ __device__ __forceinline__ T block_max_t(T v, T* red) {
     return s;   // valid in thread 0
 }
 
+// Largest block the batch kernels accept (the autotuner's largest) and the FP32 gradient's
+// minimum resident blocks at that size (its register cap).
+#ifndef FV2D_KB_MAXT
+#define FV2D_KB_MAXT 512
+#endif
+#ifndef FV2D_KBG_MINB32
+#define FV2D_KBG_MINB32 2
+#endif
 template <class T>
-__global__ void __launch_bounds__(512, sizeof(T) == 4 ? 2 : 1)
+__global__ void __launch_bounds__(FV2D_KB_MAXT, sizeof(T) == 4 ? FV2D_KBG_MINB32 : 1)
 kb_gradient(const Tile* __restrict__ tiles, const int* __restrict__ ntiles, DevMesh<T> m,
             const SolveParams<T>* __restrict__ P, const Q4<T>* __restrict__ Qin, const Q4<T>* __restrict__ Qprev,
             const Q4<T>* __restrict__ Gprev, Q4<T>* __restrict__ Gout) {
@@ -87,7 +95,7 @@ kb_gradient(const Tile* __restrict__ tiles, const int* __restrict__ ntiles, DevM
 }
 
 template <class T, bool LAST>
-__global__ void __launch_bounds__(512, sizeof(T) == 4 ? 2 : 1)
+__global__ void __launch_bounds__(FV2D_KB_MAXT, sizeof(T) == 4 ? 2 : 1)
 kb_face(const Tile* __restrict__ tiles, const int* __restrict__ ntiles, DevMesh<T> m,
         const SolveParams<T>* __restrict__ P, const Q4<T>* __restrict__ Qin, const Q4<T>* __restrict__ G,
         Q4<T>* __restrict__ tout, T* __restrict__ sout) {
@@ -112,7 +120,7 @@ kb_face(const Tile* __restrict__ tiles, const int* __restrict__ ntiles, DevMesh<
 }
 
 template <class T, int STAGE>
-__global__ void __launch_bounds__(512)
+__global__ void __launch_bounds__(FV2D_KB_MAXT)
 kb_update(const Tile* __restrict__ tiles, const int* __restrict__ ntiles, DevMesh<T> m, SolveParams<T>* P,
           const Q4<T>* __restrict__ tface, const T* __restrict__ sface, Q4<T>* __restrict__ Qn, Q4<T>* __restrict__ Q1,
           Q4<T>* __restrict__ Q2, T* __restrict__ dt, T* __restrict__ S, T* __restrict__ smax, double* __restrict__ res2,

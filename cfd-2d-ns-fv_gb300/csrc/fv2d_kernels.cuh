@@ -254,8 +254,11 @@ __device__ __forceinline__ void gradient_cell(int c, const DevMesh<T>& m, const 
 template <class T>
 constexpr int kStageBlock = sizeof(T) == 4 ? 256 : FV2D_FP64_BLOCK;   // gradient and face kernels
 
+#ifndef FV2D_KG_MINB32
+#define FV2D_KG_MINB32 4   // 61 registers, no spills: 3.5 % faster than 5 blocks at 48 registers
+#endif
 template <class T, bool SQUEEZE>
-__global__ void __launch_bounds__(kStageBlock<T>, sizeof(T) == 4 ? 5 : FV2D_FP64_GMINB)
+__global__ void __launch_bounds__(kStageBlock<T>, sizeof(T) == 4 ? FV2D_KG_MINB32 : FV2D_FP64_GMINB)
 k_gradient(int nc, DevMesh<T> m, const Q4<T>* __restrict__ Q, const Q4<T>* __restrict__ Qprev,
            const Q4<T>* __restrict__ Gprev, Q4<T>* __restrict__ Gout, Consts<T> k, int first_stage, int init_prims) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -472,6 +475,28 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
     e = (a - (s - bp)) + (b - bp);
 }
 
+// Incidences whose loads the residual gather issues together: 4 for FP64 (4.6 % faster k_update);
+// 1 for FP32, where the wider chunk's registers cost the batch kernel more than it gains.
+template <class T>
+constexpr int kUpdChunk = sizeof(T) == 8 ? 4 : 1;
+
+// S_c = sum of the face spectral terms in CSR order, loads issued a chunk at a time
+template <class T>
+__device__ __forceinline__ T spectral_sum(const int* __restrict__ inc, const T* __restrict__ sface, int b, int e) {
+    T s = T(0);
+    constexpr int U = kUpdChunk<T>;
+    for (int i0 = b; i0 < e; i0 += U) {
+        T v[U];
+#pragma unroll
+        for (int u = 0; u < U; u++)
+            if (i0 + u < e) v[u] = sface[inc[i0 + u] >> 1];
+#pragma unroll
+        for (int u = 0; u < U; u++)
+            if (i0 + u < e) s += v[u];
+    }
+    return s;
+}
+
 template <class T, int STAGE>
 __device__ __forceinline__ T update_cell(int c, const DevMesh<T>& m, const Q4<T>* __restrict__ tface,
                                          const T* __restrict__ sface, Q4<T>* __restrict__ Qn, Q4<T>* __restrict__ Q1,
@@ -483,15 +508,29 @@ __device__ __forceinline__ T update_cell(int c, const DevMesh<T>& m, const Q4<T>
 #pragma unroll
     for (int j = 0; j < 4; j++) r[j] = T(0);
     const int b = m.inc_off[c], e = m.inc_off[c + 1];
-    for (int i = b; i < e; i++) {
-        const int f = inc[i] >> 1;
-        const Q4<T> t = ldq(tface, f);
-        if (inc[i] & 1) {
+    // chunks of kUpdChunk incidences: every record and face contribution of a chunk is requested
+    // before the first is summed (more loads in flight per thread); the sums keep CSR order
+    constexpr int U = kUpdChunk<T>;
+    for (int i0 = b; i0 < e; i0 += U) {
+        int iv[U];
+        Q4<T> tv[U];
 #pragma unroll
-            for (int j = 0; j < 4; j++) r[j] -= t.p[j];
-        } else {
+        for (int u = 0; u < U; u++)
+            if (i0 + u < e) iv[u] = inc[i0 + u];
 #pragma unroll
-            for (int j = 0; j < 4; j++) r[j] += t.p[j];
+        for (int u = 0; u < U; u++)
+            if (i0 + u < e) tv[u] = ldq(tface, iv[u] >> 1);
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            if (i0 + u < e) {
+                if (iv[u] & 1) {
+#pragma unroll
+                    for (int j = 0; j < 4; j++) r[j] -= tv[u].p[j];
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 4; j++) r[j] += tv[u].p[j];
+                }
+            }
         }
     }
     const T vc = m.vol[c];
@@ -535,7 +574,7 @@ __device__ __forceinline__ T update_cell(int c, const DevMesh<T>& m, const Q4<T>
                 }
                 Qn[c] = out;
                 Qlo[c] = lo;
-                for (int i = b; i < e; i++) snext += sface[inc[i] >> 1];
+                snext = spectral_sum(inc, sface, b, e);
                 S[c] = snext;
             }
             if (!(out.p[0] > T(0)) || !(out.p[3] > T(0))) atomicOr(flag, 1);
@@ -557,7 +596,7 @@ __device__ __forceinline__ T update_cell(int c, const DevMesh<T>& m, const Q4<T>
         for (int j = 0; j < 4; j++)
             out.p[j] = T(1.0 / 3.0) * qn.p[j] + T(2.0 / 3.0) * q2.p[j] + T(2.0 / 3.0) * dtc * r[j];
         Qn[c] = out;
-        for (int i = b; i < e; i++) snext += sface[inc[i] >> 1];
+        snext = spectral_sum(inc, sface, b, e);
         S[c] = snext;
     }
     if (!(out.p[0] > T(0)) || !(out.p[3] > T(0))) atomicOr(flag, 1);

@@ -7,6 +7,7 @@
 #include <cstring>
 #include <vector>
 
+#include "fv2d_hostcopy.h"
 #include "fv2d_kernels.cuh"
 #include "fv2d_solver.h"
 
@@ -30,6 +31,8 @@ public:
         for (auto e : free_events_) cudaEventDestroy(e);
         if (arena_) cudaFree(arena_);
         if (host_stage_) cudaFreeHost(host_stage_);
+        for (cudaEvent_t e : copy_events_) cudaEventDestroy(e);
+        if (stage_free_) cudaEventDestroy(stage_free_);
         if (stream_) cudaStreamDestroy(stream_);
     }
 
@@ -105,6 +108,7 @@ public:
         staging_bytes_ = std::max<size_t>({sizeof(T) * (size_t)nf_, 8 * (size_t)nc_ * 8, 4 * (size_t)ninc_,
                                            4 * (size_t)(nc_ + 1), 4 * (size_t)nf_});
         FV2D_CUDA(cudaMallocHost(&host_stage_, staging_bytes_));
+        FV2D_CUDA(cudaEventCreateWithFlags(&stage_free_, cudaEventDisableTiming));
         auto put = [&](void* dst, const void* src, size_t bytes) -> int {
             std::memcpy(host_stage_, src, bytes);
             FV2D_CUDA(cudaMemcpyAsync(dst, host_stage_, bytes, cudaMemcpyHostToDevice, stream_));
@@ -152,8 +156,7 @@ public:
     }
 
     int upload_state(const double* q) {
-        std::memcpy(host_stage_, q, 8 * 4 * (size_t)nc_);
-        FV2D_CUDA(cudaMemcpyAsync(dstage_, host_stage_, 8 * 4 * (size_t)nc_, cudaMemcpyHostToDevice, stream_));
+        FV2D_CUDA(staged_h2d(dstage_, q, 8 * 4 * (size_t)nc_, host_stage_, stream_, stage_free_));
         launch(K_STATE_IN, nc_, [&](int gr) { k_state_in<T><<<gr, 256, 0, stream_>>>(nc_, n2o_, dstage_, Q_[0], Qlo_); });
         // fresh face histories: -101 sentinel for the limiter, initial Vn_avg/c_avg for dt
         FV2D_CUDA(cudaMemsetAsync(smax_, 0, 64, stream_));
@@ -173,8 +176,7 @@ public:
     // Qbar only; face histories and the stage counter are kept (the run continues).
     int load_state(const double* q) override {
         if (stage_ != 0) { err_ = "load_state between iterations only (stage counter is not 0)"; return FV2D_ERR_ARG; }
-        std::memcpy(host_stage_, q, 8 * 4 * (size_t)nc_);
-        FV2D_CUDA(cudaMemcpyAsync(dstage_, host_stage_, 8 * 4 * (size_t)nc_, cudaMemcpyHostToDevice, stream_));
+        FV2D_CUDA(staged_h2d(dstage_, q, 8 * 4 * (size_t)nc_, host_stage_, stream_, stage_free_));
         launch(K_STATE_IN, nc_, [&](int gr) { k_state_in<T><<<gr, 256, 0, stream_>>>(nc_, n2o_, dstage_, Q_[0], Qlo_); });
         FV2D_CUDA(cudaGetLastError());
         init_prims_ = false;
@@ -287,9 +289,7 @@ public:
                                                          field == FV2D_F_QBAR ? Qlo_ : nullptr);
             });
         const size_t bytes = 8 * (size_t)ncomp * nc_;
-        FV2D_CUDA(cudaMemcpyAsync(host_stage_, dstage_, bytes, cudaMemcpyDeviceToHost, stream_));
-        FV2D_CUDA(cudaStreamSynchronize(stream_));
-        std::memcpy(out, host_stage_, bytes);
+        FV2D_CUDA(staged_d2h(out, dstage_, bytes, host_stage_, stream_, copy_events_));
         return rc;
     }
 
@@ -386,6 +386,8 @@ private:
     void* arena_ = nullptr;
     size_t arena_bytes_ = 0;
     void* host_stage_ = nullptr;
+    std::vector<cudaEvent_t> copy_events_;   // one per staged D2H chunk
+    cudaEvent_t stage_free_ = nullptr;       // the staging buffer's last H2D has been read
     size_t staging_bytes_ = 0;
     Q4<T>* Q_[3] = {nullptr, nullptr, nullptr};
     Q4<T>* G_[3] = {nullptr, nullptr, nullptr};

@@ -167,3 +167,22 @@ def test_mesh_errors(pkg):
 def test_fp64_engine_is_built_without_fma_contraction():
     src = open(os.path.join(ROOT, "cfd-2d-ns-fv_gb300", "build.py")).read()
     assert re.search(r'"fv2d_fp64\.cu".*-fmad=false', src)
+
+
+def test_parallel_host_copy(tmp_path):
+    """The pooled host copy used by the staged host<->device transfers copies every byte."""
+    import shutil
+    import subprocess
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    cuda_inc = next((d for d in ("/usr/local/cuda/include",) if os.path.exists(os.path.join(d, "cuda_runtime.h"))), None)
+    if cuda_inc is None:
+        pytest.skip("no CUDA headers")
+    exe = str(tmp_path / "copypool_check")
+    here = os.path.dirname(os.path.abspath(__file__))
+    subprocess.run([cxx, "-std=c++17", "-O2", "-pthread", "-I", cuda_inc, "-I",
+                    os.path.join(ROOT, "cfd-2d-ns-fv_gb300", "csrc"), os.path.join(here, "cpu_helpers", "copypool_check.cpp"),
+                    "-o", exe], check=True, capture_output=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout
