@@ -16,6 +16,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <vector>
 
 #include "fv2d_batch.h"
@@ -160,6 +161,35 @@ kb_update(const Tile* __restrict__ tiles, const int* __restrict__ ntiles, DevMes
     }
 }
 
+// A newly admitted solve's ids: solve-local -> arena (CSR offsets + i0, face ids + f0, cell ids + c0;
+// negative BC codes and "no ghost cell" (-1) entries unchanged).
+template <class I>   // I = int (a template so each precision's unit may include it)
+__global__ void k_shift_ids(I* __restrict__ inc_off, int n1, I i0, I* __restrict__ inc, I* __restrict__ nbr, int k,
+                            I* __restrict__ fc1, I* __restrict__ fc2, I* __restrict__ qcell, int m, I f0, I c0) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < max(n1, max(k, m)); i += gridDim.x * blockDim.x) {
+        if (i < n1) inc_off[i] += i0;
+        if (i < k) {
+            const int v = inc[i];
+            inc[i] = (((v >> 1) + f0) << 1) | (v & 1);
+            if (nbr[i] >= 0) nbr[i] += c0;
+        }
+        if (i < m) {
+            fc1[i] += c0;
+            if (fc2[i] >= 0) fc2[i] += c0;
+            if (qcell[i] >= 0) qcell[i] += c0;
+        }
+    }
+}
+
+// A newly admitted solve's uniform initial state (and its FP32 compensation term).
+template <class T>
+__global__ void k_fill_q(Q4<T>* __restrict__ Q, Q4<T>* __restrict__ Qlo, int n, Q4<T> hi, Q4<T> lo) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        Q[i] = hi;
+        if (Qlo) Qlo[i] = lo;
+    }
+}
+
 // First-fit allocator of index ranges with coalescing frees.
 class RangeAlloc {
 public:
@@ -211,15 +241,19 @@ class BatchImpl : public Batch {
         long long c0 = 0, n = 0, f0 = 0, m = 0, i0 = 0, k = 0;
         std::vector<int> n2o;
         int iterations = 0;
+        std::shared_ptr<void> image;   // the mesh's upload image (source of in-flight copies)
     };
 
 public:
     ~BatchImpl() override {
+        if (stream_) cudaStreamSynchronize(stream_);   // copies from the solves' images may be in flight
         if (graph_) cudaGraphExecDestroy(graph_);
         for (auto& p : pending_) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
         for (auto e : free_events_) cudaEventDestroy(e);
         if (arena_) cudaFree(arena_);
-        if (pin_) cudaFreeHost(pin_);
+        if (tile_pin_) cudaFreeHost(tile_pin_);
+        if (pin_params_) cudaFreeHost(pin_params_);
+        if (tiles_free_) cudaEventDestroy(tiles_free_);
         if (stream_) cudaStreamDestroy(stream_);
     }
 
@@ -233,6 +267,8 @@ public:
         Ic_ = 2 * max_faces;
         S_ = max_solves;
         FV2D_B(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+        FV2D_B(cudaEventCreateWithFlags(&tiles_free_, cudaEventDisableTiming));
+        FV2D_B(cudaMallocHost(&pin_params_, sizeof(SolveParams<T>) * (size_t)max_solves));
         size_t off = 0;
         auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) & ~size_t(255); return o; };
         const size_t q4 = sizeof(Q4<T>);
@@ -290,7 +326,55 @@ public:
         HostMesh hm;
         int rc = build_mesh(d, cs, hm, err_);
         if (rc) return rc;
-        return add_mesh(hm, cs, sid_out);
+        rc = add_mesh(hm, cs, sid_out);
+        // the uploads read hm's image, which goes with hm
+        const cudaError_t e = cudaStreamSynchronize(stream_);
+        if (!rc && e != cudaSuccess) { err_ = cudaGetErrorString(e); return FV2D_ERR_CUDA; }
+        return rc;
+    }
+
+    // Upload image of one mesh: every per-solve array in arena format with solve-local ids, in one
+    // page-locked block, so an admission is a few asynchronous copies plus an id-shift kernel.
+    struct MeshImage {
+        long long n = 0, m = 0, k = 0;
+        char* pin = nullptr;
+        size_t o_off = 0, o_inc = 0, o_nbr = 0, o_fc1 = 0, o_fc2 = 0, o_qc = 0, o_ixx = 0, o_iyy = 0, o_ixy = 0,
+               o_vol = 0, o_igeo = 0, o_geo[14] = {};
+        std::vector<int> n2o;
+        ~MeshImage() { if (pin) cudaFreeHost(pin); }
+    };
+
+    int mesh_image(const HostMesh& hm, std::shared_ptr<MeshImage>& out) {
+        auto& slot = hm.batch_image[sizeof(T) == 4 ? 1 : 0];
+        if (slot) { out = std::static_pointer_cast<MeshImage>(slot); return FV2D_OK; }
+        DeviceLayout L;
+        build_layout(hm, L);
+        auto im = std::make_shared<MeshImage>();
+        im->n = hm.nc; im->m = hm.nf; im->k = L.ninc;
+        size_t off = 0;
+        auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 63) & ~size_t(63); return o; };
+        const size_t n = (size_t)im->n, m = (size_t)im->m, k = (size_t)im->k;
+        im->o_off = take(4 * (n + 1)); im->o_inc = take(4 * k); im->o_nbr = take(4 * k);
+        im->o_fc1 = take(4 * m); im->o_fc2 = take(4 * m); im->o_qc = take(4 * m);
+        im->o_ixx = take(8 * n); im->o_iyy = take(8 * n); im->o_ixy = take(8 * n);
+        im->o_vol = take(sizeof(T) * n); im->o_igeo = take(sizeof(T) * 4 * k);
+        for (int gI = 0; gI < 14; gI++) im->o_geo[gI] = take(sizeof(T) * m);
+        FV2D_B(cudaMallocHost(&im->pin, off));
+        auto cp = [&](size_t o, const void* src, size_t bytes) { std::memcpy(im->pin + o, src, bytes); };
+        auto cpT = [&](size_t o, const std::vector<double>& src) {
+            T* d = (T*)(im->pin + o);
+            for (size_t i = 0; i < src.size(); i++) d[i] = (T)src[i];
+        };
+        cp(im->o_off, L.inc_off.data(), 4 * (n + 1)); cp(im->o_inc, L.inc.data(), 4 * k);
+        cp(im->o_nbr, L.nbr.data(), 4 * k); cp(im->o_fc1, L.fc1.data(), 4 * m); cp(im->o_fc2, L.fc2.data(), 4 * m);
+        cp(im->o_qc, L.qcell.data(), 4 * m);
+        cp(im->o_ixx, L.Ixx.data(), 8 * n); cp(im->o_iyy, L.Iyy.data(), 8 * n); cp(im->o_ixy, L.Ixy.data(), 8 * n);
+        cpT(im->o_vol, L.vol); cpT(im->o_igeo, L.igeo);
+        for (int gI = 0; gI < 14; gI++) cpT(im->o_geo[gI], L.fgeo[gI]);
+        im->n2o = hm.cell_new2old;
+        slot = im;
+        out = im;
+        return FV2D_OK;
     }
 
     int add_mesh(const HostMesh& hm, const fv2d_case* cs, int* sid_out) override {
@@ -298,37 +382,45 @@ public:
         int sid = -1;
         for (int i = 0; i < S_; i++) if (!recs_[i].active) { sid = i; break; }
         if (sid < 0) { err_ = "batch is full (max solves)"; return FV2D_ERR_NOMEM; }
-        int rc;
-        DeviceLayout L;
-        build_layout(hm, L);
+        std::shared_ptr<MeshImage> im;
+        int rc = mesh_image(hm, im);
+        if (rc) return rc;
         Rec r;
-        r.n = hm.nc; r.m = hm.nf; r.k = L.ninc;
+        r.n = im->n; r.m = im->m; r.k = im->k;
         if (!cells_.alloc(r.n + 1, &r.c0)) { err_ = "batch cell capacity exhausted"; return FV2D_ERR_NOMEM; }
         if (!faces_.alloc(r.m, &r.f0)) { cells_.release(r.c0, r.n + 1); err_ = "batch face capacity exhausted"; return FV2D_ERR_NOMEM; }
         if (!incs_.alloc(r.k, &r.i0)) {
             cells_.release(r.c0, r.n + 1); faces_.release(r.f0, r.m);
             err_ = "batch incidence capacity exhausted"; return FV2D_ERR_NOMEM;
         }
-        // shift local ids to arena ids
-        for (auto& v : L.inc_off) v += (int)r.i0;
-        for (auto& v : L.inc) v = (((v >> 1) + (int)r.f0) << 1) | (v & 1);
-        for (auto& v : L.nbr) if (v >= 0) v += (int)r.c0;
-        for (auto& v : L.fc1) v += (int)r.c0;
-        for (auto& v : L.fc2) if (v >= 0) v += (int)r.c0;
-        for (auto& v : L.qcell) if (v >= 0) v += (int)r.c0;
-        const size_t n = (size_t)r.n;
-        if ((rc = put(m_.inc_off + r.c0, L.inc_off.data(), 4 * (n + 1)))) return rc;
-        if ((rc = put(m_.inc + r.i0, L.inc.data(), 4 * (size_t)r.k))) return rc;
-        if ((rc = put(m_.nbr + r.i0, L.nbr.data(), 4 * (size_t)r.k))) return rc;
-        if ((rc = put(m_.fc1 + r.f0, L.fc1.data(), 4 * (size_t)r.m))) return rc;
-        if ((rc = put(m_.fc2 + r.f0, L.fc2.data(), 4 * (size_t)r.m))) return rc;
-        if ((rc = put(m_.qcell + r.f0, L.qcell.data(), 4 * (size_t)r.m))) return rc;
-        if ((rc = put(m_.Ixx + r.c0, L.Ixx.data(), 8 * n))) return rc;
-        if ((rc = put(m_.Iyy + r.c0, L.Iyy.data(), 8 * n))) return rc;
-        if ((rc = put(m_.Ixy + r.c0, L.Ixy.data(), 8 * n))) return rc;
-        if ((rc = putT((T*)m_.vol + r.c0, L.vol))) return rc;
-        if ((rc = putT((T*)m_.igeo + 4 * r.i0, L.igeo))) return rc;
-        for (int gI = 0; gI < 14; gI++) if ((rc = putT(geo_[gI] + r.f0, L.fgeo[gI]))) return rc;
+        // asynchronous copies from the page-locked image (it outlives them: it is freed only with
+        // the mesh, and a solve's mesh stays alive while it is admitted or the caller synchronises)
+        const size_t n = (size_t)r.n, m = (size_t)r.m, k = (size_t)r.k;
+        const char* P = im->pin;
+        auto up = [&](const void* dst, size_t o, size_t bytes) {
+            return cudaMemcpyAsync(const_cast<void*>(dst), P + o, bytes, cudaMemcpyHostToDevice, stream_);
+        };
+        FV2D_B(up(m_.inc_off + r.c0, im->o_off, 4 * (n + 1)));
+        FV2D_B(up(m_.inc + r.i0, im->o_inc, 4 * k));
+        FV2D_B(up(m_.nbr + r.i0, im->o_nbr, 4 * k));
+        FV2D_B(up(m_.fc1 + r.f0, im->o_fc1, 4 * m));
+        FV2D_B(up(m_.fc2 + r.f0, im->o_fc2, 4 * m));
+        FV2D_B(up(m_.qcell + r.f0, im->o_qc, 4 * m));
+        FV2D_B(up(m_.Ixx + r.c0, im->o_ixx, 8 * n));
+        FV2D_B(up(m_.Iyy + r.c0, im->o_iyy, 8 * n));
+        FV2D_B(up(m_.Ixy + r.c0, im->o_ixy, 8 * n));
+        FV2D_B(up(m_.vol + r.c0, im->o_vol, sizeof(T) * n));
+        FV2D_B(up(m_.igeo + r.i0, im->o_igeo, sizeof(T) * 4 * k));
+        for (int gI = 0; gI < 14; gI++) FV2D_B(up(geo_[gI] + r.f0, im->o_geo[gI], sizeof(T) * m));
+        // solve-local ids -> arena ids, on the device
+        {
+            const long long mx = std::max<long long>({r.n + 1, r.k, r.m});
+            const int gr = (int)std::min<long long>((mx + 255) / 256, 4LL * sms_);
+            k_shift_ids<int><<<gr, 256, 0, stream_>>>((int*)m_.inc_off + r.c0, (int)(r.n + 1), (int)r.i0, (int*)m_.inc + r.i0,
+                                                (int*)m_.nbr + r.i0, (int)r.k, (int*)m_.fc1 + r.f0, (int*)m_.fc2 + r.f0,
+                                                (int*)m_.qcell + r.f0, (int)r.m, (int)r.f0, (int)r.c0);
+            FV2D_B(cudaGetLastError());
+        }
         // parameters and the uniform freestream state (main.cpp:75-118)
         SolveParams<T> p{};
         const double gm1 = cs->gamma - 1, Cp = cs->R * cs->gamma / (cs->gamma - 1), kc = (cs->mu * Cp) / cs->Pr;
@@ -341,28 +433,29 @@ public:
         p.k.c0 = (T)std::sqrt(cs->gamma * (cs->P / cs->rho));
         p.order2 = cs->order == 2; p.ns = cs->eqn == FV2D_NS; p.squeeze = cs->limiter == FV2D_LIM_SQUEEZE;
         p.global_dt = cs->time_type == FV2D_DT_GLOBAL; p.fresh = 1; p.init_prims = 1;
-        if ((rc = put(P_ + sid, &p, sizeof(p)))) return rc;
+        pin_params_[sid] = p;   // a slot is rewritten only after its solve was removed (synchronised)
+        FV2D_B(cudaMemcpyAsync(P_ + sid, pin_params_ + sid, sizeof(p), cudaMemcpyHostToDevice, stream_));
         // as the single-solve upload: hi = the state rounded to T, lo = the rounded remainder
         const double qd[4] = {cs->rho, cs->rho * cs->u, cs->rho * cs->v, E};
         Q4<T> hi1, lo1;
         for (int j = 0; j < 4; j++) { hi1.p[j] = (T)qd[j]; lo1.p[j] = (T)(qd[j] - (double)hi1.p[j]); }
-        std::vector<Q4<T>> q(n, hi1);
-        if ((rc = put(Q_[0] + r.c0, q.data(), sizeof(Q4<T>) * n))) return rc;
-        if (Qlo_) {
-            std::fill(q.begin(), q.end(), lo1);
-            if ((rc = put(Qlo_ + r.c0, q.data(), sizeof(Q4<T>) * n))) return rc;
+        {
+            const int gr = (int)std::min<long long>((r.n + 255) / 256, 4LL * sms_);
+            k_fill_q<T><<<gr, 256, 0, stream_>>>(Q_[0] + r.c0, Qlo_ ? Qlo_ + r.c0 : nullptr, (int)r.n, hi1, lo1);
+            FV2D_B(cudaGetLastError());
         }
-        int zero = 0;
-        if ((rc = put(flags_ + sid, &zero, 4))) return rc;
+        FV2D_B(cudaMemsetAsync(flags_ + sid, 0, 4, stream_));
         FV2D_B(cudaMemsetAsync(smax_ + sid, 0, sizeof(T), stream_));
         k_spectral_init<T><<<(int)((n + 255) / 256), 256, 0, stream_>>>((int)n, m_.inc_off + r.c0, m_.inc, m_.g.area,
                                                                          S_arr_ + r.c0, smax_ + sid, p.k);
         FV2D_B(cudaGetLastError());
-        r.n2o = hm.cell_new2old;
+        r.n2o = im->n2o;
+        r.image = im;   // keeps the copies' source alive until the solve is removed
         r.active = true;
         recs_[sid] = std::move(r);
         *sid_out = sid;
-        return rebuild_tiles();
+        tiles_dirty_ = true;   // rebuilt once before the next step, after every admission of a round
+        return FV2D_OK;
     }
 
     int remove(int sid) override {
@@ -373,11 +466,16 @@ public:
         faces_.release(r.f0, r.m);
         incs_.release(r.i0, r.k);
         r = Rec();
-        return rebuild_tiles();
+        tiles_dirty_ = true;
+        return FV2D_OK;
     }
 
     int step(int iterations) override {
         if (iterations < 0) { err_ = "negative iteration count"; return FV2D_ERR_ARG; }
+        if (tiles_dirty_) {
+            const int rc = rebuild_tiles();
+            if (rc) return rc;
+        }
         if (n_ctiles_ == 0) return FV2D_OK;
         for (int it = 0; it < iterations; it++) {
             if (timing_) {
@@ -479,33 +577,12 @@ public:
     void* stream() override { return (void*)stream_; }
 
 private:
-    int put(const void* dst_c, const void* src, size_t bytes) {
-        void* dst = const_cast<void*>(dst_c);
-        if (bytes == 0) return FV2D_OK;
-        if (bytes > pin_bytes_) {
-            if (pin_) cudaFreeHost(pin_);
-            pin_ = nullptr;
-            pin_bytes_ = 0;
-            FV2D_B(cudaMallocHost(&pin_, bytes));
-            pin_bytes_ = bytes;
-        }
-        FV2D_B(cudaStreamSynchronize(stream_));
-        std::memcpy(pin_, src, bytes);
-        FV2D_B(cudaMemcpyAsync(dst, pin_, bytes, cudaMemcpyHostToDevice, stream_));
-        FV2D_B(cudaStreamSynchronize(stream_));
-        return FV2D_OK;
-    }
-    int putT(T* dst, const std::vector<double>& src) {
-        std::vector<T> h(src.size());
-        for (size_t i = 0; i < src.size(); i++) h[i] = (T)src[i];
-        return put(dst, h.data(), sizeof(T) * h.size());
-    }
-
     int bucket(long long cells) const {
         return cells < tune_.bucket_edges[0] ? 0 : cells < tune_.bucket_edges[1] ? 1 : 2;
     }
 
     int rebuild_tiles() {
+        tiles_dirty_ = false;
         std::vector<Tile> tc, tf;
         for (int s = 0; s < S_; s++) {
             const Rec& r = recs_[s];
@@ -515,13 +592,29 @@ private:
             for (long long f = 0; f < r.m; f += tile) tf.push_back(Tile{s, (int)(r.f0 + f), (int)std::min(tile, r.m - f), 0});
         }
         if ((int)tc.size() > tile_cap_ || (int)tf.size() > tile_cap_) { err_ = "tile list capacity exceeded"; return FV2D_ERR_NOMEM; }
-        int rc;
-        if (!tc.empty() && (rc = put(tc_, tc.data(), sizeof(Tile) * tc.size()))) return rc;
-        if (!tf.empty() && (rc = put(tf_, tf.data(), sizeof(Tile) * tf.size()))) return rc;
-        int cnt[2] = {(int)tc.size(), (int)tf.size()};
-        if ((rc = put(cnt_, cnt, sizeof(cnt)))) return rc;
-        n_ctiles_ = cnt[0];
-        n_ftiles_ = cnt[1];
+        // asynchronous upload through a page-locked buffer; an event guards the buffer until the
+        // previous upload has been read (the graph reads the device lists in stream order)
+        const size_t bt = sizeof(Tile) * tc.size(), bf = sizeof(Tile) * tf.size(), need = bt + bf + 64;
+        FV2D_B(cudaEventSynchronize(tiles_free_));
+        if (need > tile_pin_bytes_) {
+            if (tile_pin_) cudaFreeHost(tile_pin_);
+            tile_pin_ = nullptr;
+            tile_pin_bytes_ = 0;
+            FV2D_B(cudaMallocHost(&tile_pin_, 2 * need));
+            tile_pin_bytes_ = 2 * need;
+        }
+        int* cnt = (int*)tile_pin_;
+        cnt[0] = (int)tc.size();
+        cnt[1] = (int)tf.size();
+        char* tp = tile_pin_ + 64;
+        if (bt) std::memcpy(tp, tc.data(), bt);
+        if (bf) std::memcpy(tp + bt, tf.data(), bf);
+        if (bt) FV2D_B(cudaMemcpyAsync(tc_, tp, bt, cudaMemcpyHostToDevice, stream_));
+        if (bf) FV2D_B(cudaMemcpyAsync(tf_, tp + bt, bf, cudaMemcpyHostToDevice, stream_));
+        FV2D_B(cudaMemcpyAsync(cnt_, cnt, 2 * sizeof(int), cudaMemcpyHostToDevice, stream_));
+        FV2D_B(cudaEventRecord(tiles_free_, stream_));
+        n_ctiles_ = (int)tc.size();
+        n_ftiles_ = (int)tf.size();
         if (tune_.full_grid) {   // grid sizes are baked into the captured graph
             compute_grids();
             if (graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
@@ -599,14 +692,17 @@ private:
 
     long long Nc_ = 0, Fc_ = 0, Ic_ = 0;
     int S_ = 0, sms_ = 1, tile_cap_ = 0, n_ctiles_ = 0, n_ftiles_ = 0;
+    bool tiles_dirty_ = false;
     int gg_ = 1, gf_[2] = {1, 1}, gu_[3] = {1, 1, 1};
     BatchTuning tune_;
     cudaStream_t stream_ = nullptr;
     cudaGraphExec_t graph_ = nullptr;
     void* arena_ = nullptr;
     size_t bytes_ = 0;
-    void* pin_ = nullptr;
-    size_t pin_bytes_ = 0;
+    char* tile_pin_ = nullptr;                 // page-locked staging of the tile lists
+    size_t tile_pin_bytes_ = 0;
+    cudaEvent_t tiles_free_ = nullptr;         // the last tile upload has been read
+    SolveParams<T>* pin_params_ = nullptr;     // page-locked source slot of each solve's parameters
     Q4<T>* Q_[3] = {nullptr, nullptr, nullptr};
     Q4<T>* G_[3] = {nullptr, nullptr, nullptr};
     T *dt_ = nullptr, *S_arr_ = nullptr, *s_ = nullptr, *smax_ = nullptr;

@@ -5,6 +5,7 @@
 #pragma once
 
 #include <cstdint>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -29,6 +30,9 @@ struct HostMesh {
     std::vector<double> dist, lx, ly, mx, my;
     // renumbering (device order)
     std::vector<int> cell_new2old, cell_old2new, face_new2old, face_old2new;
+    // the batch engine's upload image of this mesh (per state precision, built on first admission,
+    // freed with the mesh)
+    mutable std::shared_ptr<void> batch_image[2];
 };
 
 // Device-order arrays derived from a HostMesh (what gets uploaded).

@@ -3,7 +3,8 @@
 Requests (a mesh and flow conditions) arrive as a Poisson process.  The server keeps every
 admitted solve resident in one batch (fv2d_batch_*): it admits waiting requests in arrival order
 whenever the batch arena has room for them (the arena is sized from an HBM budget), advances all
-active solves together `check_every` iterations at a time, and retires a solve when every
+active solves together `check_every` iterations at a time (admissions are made while those
+iterations run on the GPU and join the next round), and retires a solve when every
 component of its residual L2 norm has dropped by `target` relative to its first check, when it
 reaches `max_iters`, or when its state turns non-physical.  Reported: p50/p99 time-to-converge
 (completion - arrival) of retired requests, the fraction that met the target, and aggregate
@@ -101,6 +102,15 @@ def serve(batch, stream, pool, duration, target=1e-6, max_iters=2000, check_ever
             records.append(rec)
             pending.append((rec, spec))
             idx += 1
+        # the active solves' next iterations go to the GPU first (asynchronous); admissions then
+        # overlap them - their uploads queue behind the step, and they join the next one
+        stepped = bool(active)
+        if stepped:
+            batch.step(check_every)
+            steps += 1
+            active_sum += len(active)
+            cell_stages += 3.0 * check_every * sum(a[0].cells for a in active.values())
+        admitted = 0
         while pending:                                   # FIFO admission while the arena has room
             rec, spec = pending[0]
             case = workloads.spec_case(spec)
@@ -114,16 +124,15 @@ def serve(batch, stream, pool, duration, target=1e-6, max_iters=2000, check_ever
             rec.admit = clock() - t0
             active[sid] = [rec, None]
             pending.popleft()
+            admitted += 1
         max_queue = max(max_queue, len(pending))
-        if not active:
+        if not stepped:
+            if admitted:
+                continue
             if idx >= len(stream):
                 break
             sleep(max(0.0, min(stream[idx][0] - (clock() - t0), duration - (clock() - t0))))
             continue
-        batch.step(check_every)
-        steps += 1
-        active_sum += len(active)
-        cell_stages += 3.0 * check_every * sum(a[0].cells for a in active.values())
         norms = batch.norms()
         now = clock() - t0
         for sid, (nr, it) in norms.items():
