@@ -390,11 +390,11 @@ def measure_serving(pkg, args):
     b = pkg.Batch(cells, faces, solves, precision=pkg.FP32)
     b.set_grid_mode(True)
     out = serve.serve(b, stream, pool, duration=args.serve_seconds, target=1e-6, max_iters=args.serve_max_iters,
-                      check_every=25)
+                      check_every=25, stall_iters=args.serve_stall_iters)
     usage = b.usage()
     b.close()
     base = serve.serve_one_at_a_time(stream, pool, duration=args.serve_seconds, precision=pkg.FP64, target=1e-6,
-                                     max_iters=args.serve_max_iters, check_every=25)
+                                     max_iters=args.serve_max_iters, check_every=25, stall_iters=args.serve_stall_iters)
     return {"batched_fp32": out, "baseline_fp64_one_at_a_time": base,
             "stream": {"rate_per_s": args.serve_rate, "seconds": args.serve_seconds, "requests": len(stream),
                        "cells": "log-uniform 5k-2M (snapped to a pool of %d meshes)" % args.pool_meshes},
@@ -600,6 +600,8 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=50.0)
     ap.add_argument("--serve-budget-gb", type=float, default=8.0)
     ap.add_argument("--serve-max-iters", type=int, default=2000)
+    ap.add_argument("--serve-stall-iters", type=int, default=250,
+                    help="retire a served solve whose residual has not dropped 1%% in this many iterations (0: off)")
     ap.add_argument("--pool-meshes", type=int, default=12)
     args = ap.parse_args()
     if args.warmup < 3:

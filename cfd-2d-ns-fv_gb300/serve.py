@@ -6,7 +6,9 @@ whenever the batch arena has room for them (the arena is sized from an HBM budge
 active solves together `check_every` iterations at a time (admissions are made while those
 iterations run on the GPU and join the next round), and retires a solve when every
 component of its residual L2 norm has dropped by `target` relative to its first check, when it
-reaches `max_iters`, or when its state turns non-physical.  Reported: p50/p99 time-to-converge
+reaches `max_iters`, when its state turns non-physical, or (optionally, `stall_iters`) when its
+residual has stopped dropping - the squeeze-limited scheme stalls near a few percent drop and can
+never reach a 1e-6 target, so running it to `max_iters` only delays the queue.  Reported: p50/p99 time-to-converge
 (completion - arrival) of retired requests, the fraction that met the target, and aggregate
 cell-stage updates/s.  The baseline serves the same stream one request at a time through the plain
 FP64 path (fv2d_create / fv2d_step).
@@ -37,8 +39,39 @@ class Record:
     finish: float = -1.0
     iterations: int = 0
     converged: bool = False
+    stalled: bool = False
     failed: bool = False
     state: object = None
+
+
+class Progress:
+    """Residual history of one solve.  r0 = the norms at its first check; 'converged' once every
+    component is at most target * r0; 'stalled' (with stall_iters > 0) once the best ratio so far
+    (largest component of r / r0) has not improved by the relative amount stall_gain within the
+    last stall_iters iterations; 'failed' on a non-finite norm."""
+
+    def __init__(self, target, stall_iters=0, stall_gain=0.01):
+        self.target, self.stall_iters, self.stall_gain = target, stall_iters, stall_gain
+        self.r0 = None
+        self.best = math.inf
+        self.best_it = 0
+
+    def update(self, norms, iteration):
+        if not np.all(np.isfinite(norms)):
+            return "failed"
+        if self.r0 is None:
+            self.r0 = np.maximum(norms, 1e-300)
+            self.best_it = iteration
+            return None
+        ratio = norms / self.r0
+        if np.all(ratio <= self.target):
+            return "converged"
+        worst = float(np.max(ratio))
+        if worst < self.best * (1.0 - self.stall_gain):
+            self.best, self.best_it = worst, iteration
+        elif self.stall_iters > 0 and iteration - self.best_it >= self.stall_iters:
+            return "stalled"
+        return None
 
 
 class MeshPool:
@@ -80,9 +113,10 @@ def _percentiles(vals):
 
 
 def serve(batch, stream, pool, duration, target=1e-6, max_iters=2000, check_every=25, clock=time.monotonic,
-          sleep=time.sleep, keep_states=False, records_out=None):
+          sleep=time.sleep, keep_states=False, records_out=None, stall_iters=0, stall_gain=0.01):
     """Continuous batching over `stream` [(arrival s, spec)] for `duration` seconds.  With
-    keep_states the final state of every retired solve is kept on its record (records_out)."""
+    keep_states the final state of every retired solve is kept on its record (records_out).
+    stall_iters > 0 also retires solves whose residual stopped dropping (Progress)."""
     t0 = clock()
     pending = deque()
     active = {}                # sid -> (record, r0 or None)
@@ -122,7 +156,7 @@ def serve(batch, stream, pool, duration, target=1e-6, max_iters=2000, check_ever
                     break
                 raise
             rec.admit = clock() - t0
-            active[sid] = [rec, None]
+            active[sid] = [rec, Progress(target, stall_iters, stall_gain)]
             pending.popleft()
             admitted += 1
         max_queue = max(max_queue, len(pending))
@@ -138,20 +172,13 @@ def serve(batch, stream, pool, duration, target=1e-6, max_iters=2000, check_ever
         for sid, (nr, it) in norms.items():
             if sid not in active or it == 0:
                 continue
-            ent = active[sid]
-            rec = ent[0]
+            rec, prog = active[sid]
             rec.iterations = it
-            done = False
-            if not np.all(np.isfinite(nr)):
-                rec.failed = True
-                done = True
-            elif ent[1] is None:
-                ent[1] = np.maximum(nr, 1e-300)
-            elif np.all(nr <= target * ent[1]):
-                rec.converged = True
-                done = True
-            if it >= max_iters:
-                done = True
+            status = prog.update(nr, it)
+            rec.failed = status == "failed"
+            rec.converged = status == "converged"
+            rec.stalled = status == "stalled"
+            done = status is not None or it >= max_iters
             if done:
                 rec.finish = now
                 if keep_states:
@@ -169,16 +196,16 @@ def serve(batch, stream, pool, duration, target=1e-6, max_iters=2000, check_ever
     p50, p99 = _percentiles(ttc)
     w50, w99 = _percentiles([r.admit - r.arrival for r in records if r.admit >= 0])
     return dict(mode="continuous batching", duration_s=round(elapsed, 2), arrived=len(records), admitted=sum(r.admit >= 0 for r in records),
-                completed=len(finished), converged=sum(r.converged for r in finished), failed=sum(r.failed for r in finished),
-                in_flight=len(active), queued=len(pending), max_queue=max_queue,
+                completed=len(finished), converged=sum(r.converged for r in finished), stalled=sum(r.stalled for r in finished),
+                failed=sum(r.failed for r in finished), in_flight=len(active), queued=len(pending), max_queue=max_queue,
                 mean_active=round(active_sum / steps, 1) if steps else 0,
                 ttc_p50_s=p50, ttc_p99_s=p99, wait_p50_s=w50, wait_p99_s=w99,
                 cell_stage_per_s=cell_stages / elapsed if elapsed > 0 else 0.0,
-                target=target, max_iters=max_iters, check_every=check_every)
+                target=target, max_iters=max_iters, check_every=check_every, stall_iters=stall_iters)
 
 
 def serve_one_at_a_time(stream, pool, duration, precision=fv2d.FP64, target=1e-6, max_iters=2000, check_every=25,
-                        clock=time.monotonic, sleep=time.sleep):
+                        clock=time.monotonic, sleep=time.sleep, stall_iters=0, stall_gain=0.01):
     """The baseline: the same stream, one request at a time, each through fv2d_create/fv2d_step."""
     t0 = clock()
     records = []
@@ -196,7 +223,7 @@ def serve_one_at_a_time(stream, pool, duration, precision=fv2d.FP64, target=1e-6
         rec = Record(rid=idx, arrival=arr, cells=int(pool.cells[i]), admit=now)
         records.append(rec)
         s = fv2d.Solver(pool.grids[i], workloads.spec_case(spec), precision=precision)
-        r0 = None
+        prog = Progress(target, stall_iters, stall_gain)
         while clock() - t0 < duration:
             s.step(check_every)
             cell_stages += 3.0 * check_every * rec.cells
@@ -206,18 +233,14 @@ def serve_one_at_a_time(stream, pool, duration, precision=fv2d.FP64, target=1e-6
             except fv2d.Fv2dError:
                 rec.failed = True
                 break
-            if not np.all(np.isfinite(nr)):
-                rec.failed = True
-                break
-            if r0 is None:
-                r0 = np.maximum(nr, 1e-300)
-            elif np.all(nr <= target * r0):
-                rec.converged = True
-                break
-            if rec.iterations >= max_iters:
+            status = prog.update(nr, rec.iterations)
+            rec.failed = status == "failed"
+            rec.converged = status == "converged"
+            rec.stalled = status == "stalled"
+            if status is not None or rec.iterations >= max_iters:
                 break
         s.close()
-        if clock() - t0 < duration or rec.converged or rec.failed or rec.iterations >= max_iters:
+        if clock() - t0 < duration or rec.converged or rec.stalled or rec.failed or rec.iterations >= max_iters:
             rec.finish = clock() - t0
         idx += 1
     elapsed = clock() - t0
@@ -226,9 +249,10 @@ def serve_one_at_a_time(stream, pool, duration, precision=fv2d.FP64, target=1e-6
     p50, p99 = _percentiles([r.finish - r.arrival for r in finished])
     return dict(mode="one at a time", precision="fp64" if precision == fv2d.FP64 else "fp32",
                 duration_s=round(elapsed, 2), arrived=arrived, completed=len(finished),
-                converged=sum(r.converged for r in finished), failed=sum(r.failed for r in finished),
+                converged=sum(r.converged for r in finished), stalled=sum(r.stalled for r in finished),
+                failed=sum(r.failed for r in finished),
                 ttc_p50_s=p50, ttc_p99_s=p99, cell_stage_per_s=cell_stages / elapsed if elapsed > 0 else 0.0,
-                target=target, max_iters=max_iters, check_every=check_every)
+                target=target, max_iters=max_iters, check_every=check_every, stall_iters=stall_iters)
 
 
 MAX_ARENA_FACES = (1 << 29) - (1 << 20)    # face ids are 32-bit (face << 1 | side) in the arena

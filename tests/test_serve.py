@@ -97,3 +97,41 @@ def test_serve_capacity_gates_admission(pkg):
                       clock=clock, sleep=clock.sleep)
     assert out["max_queue"] == 3
     assert out["completed"] == 5 and out["converged"] == 0       # retired at the iteration cap
+
+
+def test_progress_converged_stalled_failed(pkg):
+    from fv2d_gb300 import serve
+    p = serve.Progress(1e-6, stall_iters=100, stall_gain=0.01)
+    assert p.update(np.full(4, 10.0), 25) is None               # r0
+    assert p.update(np.full(4, 5.0), 50) is None                # improving
+    assert p.update(np.full(4, 4.99), 100) is None              # < 1 % better: best stays at it 50
+    assert p.update(np.full(4, 5.0), 150) == "stalled"          # 100 iterations without a 1 % gain
+    q = serve.Progress(1e-6)
+    q.update(np.full(4, 1.0), 25)
+    assert q.update(np.full(4, 1e-7), 50) == "converged"
+    assert q.update(np.array([1.0, np.nan, 1.0, 1.0]), 75) == "failed"
+    never = serve.Progress(1e-6, stall_iters=0)                   # stall detection off
+    never.update(np.full(4, 1.0), 25)
+    assert all(never.update(np.full(4, 1.0), it) is None for it in range(50, 5000, 25))
+
+
+class StallingBatch(FakeBatch):
+    """Residuals drop to 5 % and stay there (the squeeze limiter's stall)."""
+
+    def norms(self):
+        return {sid: (np.full(4, max(0.05, 10.0 ** (-s[1] / 20))), s[1]) for sid, s in self.solves.items()}
+
+
+def test_serve_retires_stalled_solves(pkg):
+    from fv2d_gb300 import serve, workloads
+    clock = FakeClock()
+    pool = FakePool([5e3, 5e4])
+    stream = workloads.c5_stream(rate=10.0, duration=3.0, seed=5, lo=5e3, hi=5e4)
+    batch = StallingBatch(capacity=10 ** 6, clock=clock, err=pkg.Fv2dError)
+    recs = []
+    out = serve.serve(batch, stream, pool, duration=60.0, target=1e-6, max_iters=5000, check_every=25,
+                      clock=clock, sleep=clock.sleep, records_out=recs, stall_iters=200)
+    done = [r for r in recs if r.finish >= 0]
+    assert done and all(r.stalled and not r.converged for r in done)
+    assert all(r.iterations < 1000 for r in done)                # well before max_iters
+    assert out["stalled"] == len(done) and out["converged"] == 0
