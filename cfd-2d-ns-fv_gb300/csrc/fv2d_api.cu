@@ -6,12 +6,21 @@
 #include <string>
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>   // header-only; ranges are free unless a profiler attaches
 
 #include "fv2d_gpu.h"
 #include "fv2d_host.h"
 #include "fv2d_output.h"
 #include "fv2d_batch.h"
 #include "fv2d_solver.h"
+
+namespace {
+// Named NVTX range around a C-ABI call (shows the library's calls on an Nsight timeline).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+};
+}  // namespace
 
 namespace fv2d {
 const char* const kKernelNames[K_COUNT] = {"k_gradient", "k_face", "k_update", "k_spectral_init",
@@ -146,6 +155,7 @@ int fv2d_mesh_permutation(const fv2d_mesh* mm, int kind, int* out) {
 }
 
 int fv2d_create(const fv2d_mesh_desc* desc, const fv2d_case* cs, int precision, fv2d_handle** out) {
+    NvtxRange nvtx_("fv2d_create");
     if (!out) return fail(FV2D_ERR_ARG, "null output");
     *out = nullptr;
     int rc = check_case(cs);
@@ -186,22 +196,25 @@ void fv2d_destroy(fv2d_handle* h) { delete h; }
 #define FV2D_H(h) if (!(h) || !(h)->s) return fail(FV2D_ERR_ARG, "null handle")
 #define FV2D_RET(h, expr) do { int rc_ = (expr); if (rc_) g_err = (h)->s->err_; return rc_; } while (0)
 
-int fv2d_step(fv2d_handle* h, int iterations) { FV2D_H(h); FV2D_RET(h, h->s->step(iterations)); }
-int fv2d_stage(fv2d_handle* h) { FV2D_H(h); FV2D_RET(h, h->s->stage()); }
+int fv2d_step(fv2d_handle* h, int iterations) { NvtxRange r("fv2d_step"); FV2D_H(h); FV2D_RET(h, h->s->step(iterations)); }
+int fv2d_stage(fv2d_handle* h) { NvtxRange r("fv2d_stage"); FV2D_H(h); FV2D_RET(h, h->s->stage()); }
 
 int fv2d_set_state(fv2d_handle* h, const double* q) {
+    NvtxRange nvtx_("fv2d_set_state");
     FV2D_H(h);
     if (!q) return fail(FV2D_ERR_ARG, "null state");
     FV2D_RET(h, h->s->set_state(q));
 }
 
 int fv2d_load_state(fv2d_handle* h, const double* q) {
+    NvtxRange nvtx_("fv2d_load_state");
     FV2D_H(h);
     if (!q) return fail(FV2D_ERR_ARG, "null state");
     FV2D_RET(h, h->s->load_state(q));
 }
 
 int fv2d_get_state(fv2d_handle* h, double* q) {
+    NvtxRange nvtx_("fv2d_get_state");
     FV2D_H(h);
     if (!q) return fail(FV2D_ERR_ARG, "null output");
     FV2D_RET(h, h->s->get_field(FV2D_F_QBAR, q));
@@ -229,6 +242,7 @@ int fv2d_sizes(fv2d_handle* h, int* o) {
 }
 
 int fv2d_save(fv2d_handle* h, int ndx) {
+    NvtxRange nvtx_("fv2d_save");
     FV2D_H(h);
     const int N = h->s->mesh_.nc;
     std::vector<double> q(4 * (size_t)N), g(8 * (size_t)N), r(4 * (size_t)N);
@@ -249,6 +263,18 @@ int fv2d_post(fv2d_handle* h, int ndx) {
     if (rc && rc != FV2D_ERR_STATE) return fail(rc, h->s->err_);
     std::string err;
     int wrc = fv2d::write_restart(h->s->mesh_, ndx, q.data(), "sol", err);
+    if (wrc) return fail(wrc, err);
+    return rc;
+}
+
+int fv2d_write_restart(fv2d_handle* h, const char* path, int ndx, int digits) {
+    FV2D_H(h);
+    if (!path || digits < 0 || digits > 17) return fail(FV2D_ERR_ARG, "bad argument");
+    std::vector<double> q(4 * (size_t)h->s->mesh_.nc);
+    int rc = h->s->get_field(FV2D_F_QBAR, q.data());
+    if (rc && rc != FV2D_ERR_STATE) return fail(rc, h->s->err_);
+    std::string err;
+    int wrc = fv2d::write_restart_file(h->s->mesh_, path, ndx, q.data(), digits, err);
     if (wrc) return fail(wrc, err);
     return rc;
 }
@@ -338,6 +364,7 @@ int fv2d_batch_footprint(const fv2d_mesh_desc* d, int precision, long long* byte
 }
 
 int fv2d_batch_add(fv2d_batch* b, const fv2d_mesh_desc* desc, const fv2d_case* cs, int* solve_id) {
+    NvtxRange nvtx_("fv2d_batch_add");
     FV2D_BH(b);
     if (!solve_id) return fail(FV2D_ERR_ARG, "null output");
     int rc = check_case(cs);
@@ -346,6 +373,7 @@ int fv2d_batch_add(fv2d_batch* b, const fv2d_mesh_desc* desc, const fv2d_case* c
 }
 
 int fv2d_batch_add_mesh(fv2d_batch* b, const fv2d_mesh* mesh, const fv2d_case* cs, int* solve_id) {
+    NvtxRange nvtx_("fv2d_batch_add_mesh");
     FV2D_BH(b);
     if (!mesh || !solve_id) return fail(FV2D_ERR_ARG, "null argument");
     int rc = check_case(cs);
@@ -354,7 +382,7 @@ int fv2d_batch_add_mesh(fv2d_batch* b, const fv2d_mesh* mesh, const fv2d_case* c
 }
 
 int fv2d_batch_remove(fv2d_batch* b, int solve_id) { FV2D_BH(b); FV2D_BRET(b, b->b->remove(solve_id)); }
-int fv2d_batch_step(fv2d_batch* b, int iterations) { FV2D_BH(b); FV2D_BRET(b, b->b->step(iterations)); }
+int fv2d_batch_step(fv2d_batch* b, int iterations) { NvtxRange r("fv2d_batch_step"); FV2D_BH(b); FV2D_BRET(b, b->b->step(iterations)); }
 
 int fv2d_batch_norms(fv2d_batch* b, int* ids, double* norms4, int* iterations, int max, int* n) {
     FV2D_BH(b);

@@ -286,6 +286,12 @@ __device__ __forceinline__ void face_flux(int f, const DevMesh<T>& m, const Q4<T
 #pragma unroll
         for (int j = 0; j < 4; j++) { g1x.p[j] = T(0); g1y.p[j] = T(0); }
     }
+    // the right cell's loads are issued now, beside the left cell's (a boundary face, c2 < 0,
+    // loads cell c1's row instead and never uses it), so the two gathers overlap
+    const int c2l = c2 >= 0 ? c2 : c1;
+    const Q4<T> q2l = ldq(Q, c2l);
+    Q4<T> g2xl, g2yl;
+    if (ORDER2) { g2xl = ldq(G, 2 * c2l); g2yl = ldq(G, 2 * c2l + 1); }
     T L[4], Rq[4];
     {
         const T dx = g.c1dx[f], dy = g.c1dy[f];
@@ -297,8 +303,8 @@ __device__ __forceinline__ void face_flux(int f, const DevMesh<T>& m, const Q4<T
     const T lc = sqrt(k.gamma * Recip<T>::div(lP, lrho, ly));
     Q4<T> q2, g2x, g2y;
     if (c2 >= 0) {
-        q2 = ldq(Q, c2);
-        if (ORDER2) { g2x = ldq(G, 2 * c2); g2y = ldq(G, 2 * c2 + 1); }
+        q2 = q2l;
+        if (ORDER2) { g2x = g2xl; g2y = g2yl; }
         else {
 #pragma unroll
             for (int j = 0; j < 4; j++) { g2x.p[j] = T(0); g2y.p[j] = T(0); }

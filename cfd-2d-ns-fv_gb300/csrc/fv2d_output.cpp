@@ -208,15 +208,22 @@ int save_solution(const HostMesh& m, const fv2d_case& cs, int ndx, const double*
     return FV2D_OK;
 }
 
-int write_restart(const HostMesh& m, int ndx, const double* q, const std::string& dir, std::string& err) {
-    std::cout << "Writing Restart File \n";                                   // post_process.cpp:13-29
-    std::ofstream out(dir + "/restart_sol.dat");
-    if (!out.is_open()) { err = "cannot write " + dir + "/restart_sol.dat"; return FV2D_ERR_IO; }
+int write_restart_file(const HostMesh& m, const std::string& path, int ndx, const double* q, int digits,
+                       std::string& err) {
+    std::ofstream out(path);
+    if (!out.is_open()) { err = "cannot write " + path; return FV2D_ERR_IO; }
+    if (digits > 0) out.precision(digits);   // 17 round-trips every double exactly
     const int N = m.nc;
     out << ndx << " " << N << std::endl;
     for (int c = 0; c < N; c++)
         out << q[c] << " " << q[N + c] << " " << q[2 * (size_t)N + c] << " " << q[3 * (size_t)N + c] << std::endl;
+    if (!out) { err = "write failed: " + path; return FV2D_ERR_IO; }
     return FV2D_OK;
+}
+
+int write_restart(const HostMesh& m, int ndx, const double* q, const std::string& dir, std::string& err) {
+    std::cout << "Writing Restart File \n";                                   // post_process.cpp:13-29
+    return write_restart_file(m, dir + "/restart_sol.dat", ndx, q, 0, err);   // stream default: 6 digits
 }
 
 int read_restart(const char* path, int num_cells, int* ndx, double* q, std::string& err) {

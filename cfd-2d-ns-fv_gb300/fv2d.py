@@ -28,7 +28,7 @@ EXPORTS = [
     "fv2d_mesh_get", "fv2d_mesh_permutation", "fv2d_create", "fv2d_create_from_files", "fv2d_destroy",
     "fv2d_step", "fv2d_stage", "fv2d_set_state", "fv2d_load_state", "fv2d_get_state", "fv2d_get_field", "fv2d_residual_norm",
     "fv2d_sizes", "fv2d_save", "fv2d_post", "fv2d_write_history_headers", "fv2d_write_mesh_files",
-    "fv2d_read_restart", "fv2d_synchronize", "fv2d_set_store_residual", "fv2d_set_graphs", "fv2d_set_kernel_timing",
+    "fv2d_read_restart", "fv2d_write_restart", "fv2d_synchronize", "fv2d_set_store_residual", "fv2d_set_graphs", "fv2d_set_kernel_timing",
     "fv2d_kernel_times", "fv2d_stream", "fv2d_device_bytes", "fv2d_last_error", "fv2d_residual_noalloc",
     "fv2d_batch_create", "fv2d_batch_destroy", "fv2d_batch_footprint", "fv2d_batch_add", "fv2d_batch_add_mesh",
     "fv2d_batch_remove",
@@ -98,6 +98,7 @@ def library():
             "fv2d_write_history_headers": (ctypes.c_int, [vp]),
             "fv2d_write_mesh_files": (ctypes.c_int, [vp]),
             "fv2d_read_restart": (ctypes.c_int, [cp, ctypes.c_int, ip, dp]),
+            "fv2d_write_restart": (ctypes.c_int, [vp, cp, ctypes.c_int, ctypes.c_int]),
             "fv2d_synchronize": (ctypes.c_int, [vp]),
             "fv2d_set_store_residual": (ctypes.c_int, [vp, ctypes.c_int]),
             "fv2d_set_graphs": (ctypes.c_int, [vp, ctypes.c_int]),
@@ -304,6 +305,10 @@ class Solver:
     def post(self, ndx: int):
         """./sol/restart_sol.dat for iteration `ndx` (the reference's post())."""
         _check(library().fv2d_post(self.h, int(ndx)), self.h)
+
+    def write_restart(self, path: str, ndx: int, digits: int = 17):
+        """Checkpoint Qbar in the restart-file layout (17 digits: exact round trip)."""
+        _check(library().fv2d_write_restart(self.h, path.encode(), int(ndx), int(digits)), self.h)
 
     def write_history_headers(self):
         _check(library().fv2d_write_history_headers(self.h), self.h)

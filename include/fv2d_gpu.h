@@ -148,6 +148,10 @@ int fv2d_post(fv2d_handle* h, int ndx);
 int fv2d_write_history_headers(fv2d_handle* h);
 /* mesh/cell_data.dat and mesh/face_data.dat (src/base/readmesh.cpp:413-446).                  */
 int fv2d_write_mesh_files(fv2d_handle* h);
+/* Checkpoint: the current Qbar in the restart_sol.dat layout (post_process.cpp:17-27) to `path`
+ * with `digits` significant digits (0: the reference's 6; 17: every double round-trips exactly
+ * through fv2d_read_restart + fv2d_set_state).                                                 */
+int fv2d_write_restart(fv2d_handle* h, const char* path, int ndx, int digits);
 /* Read sol/restart_sol.dat-format file into q (4N SoA); *ndx = the iteration it was written at
  * (src/base/main.cpp:82-104).  Host only.                                                      */
 int fv2d_read_restart(const char* path, int num_cells, int* ndx, double* q);

@@ -104,3 +104,29 @@ def test_batch_admission(pkg):
     b.step(2)
     assert len(b.norms()) == 1
     b.close()
+
+
+def test_failing_solve_is_isolated(pkg):
+    """A solve whose state turns non-physical (CFL far beyond stability) is reported for that solve
+    alone (non-finite norms or FV2D_ERR_STATE on its state); its neighbour in the same batch keeps
+    advancing exactly as alone."""
+    mg = pkg.meshgen
+    good_grid, good_case = mix(pkg)[0]
+    bad_grid = mg.voronoi_bump_channel(4000, seed=9)
+    bad_case = dict(mg.DEFAULT_CASE, eqn="EULER", limiter="NONE", time_step_type="LOCAL", CFL=40.0,
+                    u=mg.mach_speed(0.8))
+    b = pkg.Batch(100000, 300000, 4, precision=pkg.FP64)
+    good = b.add(good_grid, good_case)
+    bad = b.add(bad_grid, bad_case)
+    b.step(30)
+    norms = b.norms()
+    failed = not np.all(np.isfinite(norms[bad][0]))
+    try:
+        b.get_state(bad)
+    except pkg.Fv2dError as e:
+        failed = failed or e.code == 7
+    assert failed, "the unstable solve was not reported"
+    assert np.all(np.isfinite(norms[good][0]))
+    q_alone, _ = alone(pkg, good_grid, good_case, 30, pkg.FP64)
+    assert bits_equal(b.get_state(good), q_alone)
+    b.close()

@@ -125,6 +125,26 @@ def test_pinned_and_pageable_transfers_agree(pkg):
     assert bits_equal(a.get_state(), b.get_state())
 
 
+def test_checkpoint_round_trip_is_exact(pkg, tmp_path):
+    """fv2d_write_restart at 17 digits + fv2d_read_restart + fv2d_set_state restores Qbar bit for
+    bit; the reference's 6-digit restart file (fv2d_post) differs from it (lossy, as in the reference)."""
+    g = pkg.meshgen.voronoi_bump_channel(5000, seed=6)
+    case = dict(pkg.meshgen.DEFAULT_CASE, u=pkg.meshgen.mach_speed(0.6), time_step_type="LOCAL")
+    s = pkg.Solver(g, case)
+    s.step(5)
+    q = s.get_state()
+    path = str(tmp_path / "ckpt.dat")
+    s.write_restart(path, 5, digits=17)
+    ndx, q2 = pkg.fv2d.read_restart(path, g.num_cells)
+    assert ndx == 5 and bits_equal(q2.ravel(), q)
+    t = pkg.Solver(g, case)
+    t.set_state(q2.ravel())
+    assert bits_equal(t.get_state(), q)
+    s.write_restart(str(tmp_path / "six.dat"), 5, digits=0)
+    _, q6 = pkg.fv2d.read_restart(str(tmp_path / "six.dat"), g.num_cells)
+    assert not bits_equal(q6.ravel(), q) and np.allclose(q6.ravel(), q, rtol=1e-5)
+
+
 def test_step_equals_stages_and_norm(pkg, orc):
     g = pkg.meshgen.channel_bump_quads(64, 32)
     case = dict(pkg.meshgen.DEFAULT_CASE, u=pkg.meshgen.mach_speed(0.5))
