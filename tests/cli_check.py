@@ -51,7 +51,7 @@ def first_difference(a: bytes, b: bytes) -> str:
     return f"line counts {len(la)} vs {len(lb)}"
 
 
-def run_case(prog_argv, case_path, work, timeout=600):
+def run_case(prog_argv, case_path, work, timeout=600, env=None):
     """Run `prog_argv` on the case in `work`; returns a list of mismatch descriptions (empty = equal)."""
     grid_txt, inputs, files = load_case(case_path)
     os.makedirs(work, exist_ok=True)
@@ -60,7 +60,7 @@ def run_case(prog_argv, case_path, work, timeout=600):
     for text in inputs:
         with open(os.path.join(work, "input.in"), "w") as fh:
             fh.write(text)
-        r = subprocess.run(list(prog_argv), cwd=work, capture_output=True, text=True, timeout=timeout)
+        r = subprocess.run(list(prog_argv), cwd=work, capture_output=True, text=True, timeout=timeout, env=env)
         if r.returncode != 0:
             return [f"{prog_argv[0]} exited {r.returncode}: {r.stderr[-1000:]}"]
     bad = []

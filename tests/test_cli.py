@@ -81,3 +81,28 @@ def test_reference_main_links_against_gpu_library(pkg, shim_program):
     assert os.path.exists(pkg.build.LIB)
     subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "shim"], check=True, capture_output=True)
     assert os.path.exists(os.path.join(ROOT, "oracle", "_ref", "fv2d_ref_shim_gpu"))
+
+
+@pytest.fixture(scope="module")
+def oracle_cli_sanitized(tmp_path_factory):
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    out = str(tmp_path_factory.mktemp("cli_san") / "cli_oracle_san")
+    cmd = [cxx, "-O1", "-g", "-std=c++17", "-ffp-contract=off", "-fsanitize=address,undefined",
+           "-fno-sanitize-recover=undefined", "-fno-omit-frame-pointer",
+           "-I", os.path.join(ROOT, "include"), "-I", CSRC, "-I", os.path.join(ROOT, "oracle"),
+           os.path.join(HERE, "cpu_helpers", "cli_oracle.cpp"), os.path.join(CSRC, "fv2d_host.cpp"),
+           os.path.join(CSRC, "fv2d_output.cpp"), os.path.join(ROOT, "oracle", "fv2d_oracle.cpp"), "-o", out]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        pytest.skip("sanitizer runtime unavailable: " + r.stderr[-300:])
+    return out
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if "airfoil" not in c], ids=lambda p: os.path.basename(p)[:-4])
+def test_host_code_clean_under_asan_ubsan(oracle_cli_sanitized, case, tmp_path):
+    """The library's host code (input/grid parsing, connectivity, geometry, renumbering, output
+    writers) has no memory errors or undefined behaviour on the golden cases (ASan + UBSan)."""
+    env = dict(os.environ, ASAN_OPTIONS="detect_leaks=0", UBSAN_OPTIONS="print_stacktrace=1")
+    assert cli_check.run_case([oracle_cli_sanitized], case, str(tmp_path), env=env) == []
