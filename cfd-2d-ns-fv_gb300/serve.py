@@ -197,7 +197,8 @@ def serve(batch, stream, pool, duration, target=1e-6, max_iters=2000, check_ever
     w50, w99 = _percentiles([r.admit - r.arrival for r in records if r.admit >= 0])
     return dict(mode="continuous batching", duration_s=round(elapsed, 2), arrived=len(records), admitted=sum(r.admit >= 0 for r in records),
                 completed=len(finished), converged=sum(r.converged for r in finished), stalled=sum(r.stalled for r in finished),
-                failed=sum(r.failed for r in finished), in_flight=len(active), queued=len(pending), max_queue=max_queue,
+                failed=sum(r.failed for r in finished), failed_requests=[r.rid for r in finished if r.failed][:32],
+                in_flight=len(active), queued=len(pending), max_queue=max_queue,
                 mean_active=round(active_sum / steps, 1) if steps else 0,
                 ttc_p50_s=p50, ttc_p99_s=p99, wait_p50_s=w50, wait_p99_s=w99,
                 cell_stage_per_s=cell_stages / elapsed if elapsed > 0 else 0.0,
@@ -250,7 +251,7 @@ def serve_one_at_a_time(stream, pool, duration, precision=fv2d.FP64, target=1e-6
     return dict(mode="one at a time", precision="fp64" if precision == fv2d.FP64 else "fp32",
                 duration_s=round(elapsed, 2), arrived=arrived, completed=len(finished),
                 converged=sum(r.converged for r in finished), stalled=sum(r.stalled for r in finished),
-                failed=sum(r.failed for r in finished),
+                failed=sum(r.failed for r in finished), failed_requests=[r.rid for r in finished if r.failed][:32],
                 ttc_p50_s=p50, ttc_p99_s=p99, cell_stage_per_s=cell_stages / elapsed if elapsed > 0 else 0.0,
                 target=target, max_iters=max_iters, check_every=check_every, stall_iters=stall_iters)
 
