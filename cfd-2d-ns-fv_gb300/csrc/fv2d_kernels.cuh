@@ -136,6 +136,12 @@ __device__ __forceinline__ void cons(T rho, T u, T v, T P, const Consts<T>& k, T
 // reconstruction at :48); they are recomputed here from the previous stage's state and limited
 // gradient with the reconstruction's own expression, or are the -101 sentinel the face states
 // start with (class_q.hpp:73-76) on the first stage after initialisation.
+// a[j] for a run-time j without indexing (which would put the array in local memory)
+template <class T>
+__device__ __forceinline__ T pick4(const T a[4], int j) {
+    return j == 0 ? a[0] : j == 1 ? a[1] : j == 2 ? a[2] : a[3];
+}
+
 template <class T, bool SQUEEZE>
 __device__ __forceinline__ void gradient_cell(int c, const DevMesh<T>& m, const Q4<T>* __restrict__ Q,
                                               const Q4<T>* __restrict__ Qprev, const Q4<T>* __restrict__ Gprev,
@@ -220,16 +226,51 @@ __device__ __forceinline__ void gradient_cell(int c, const DevMesh<T>& m, const 
         T phi[4] = {T(1), T(1), T(1), T(1)};
         Q4<T> qp, gpx, gpy;
         if (!first_stage) { qp = ldq(Qprev, c); gpx = ldq(Gprev, 2 * c); gpy = ldq(Gprev, 2 * c + 1); }
-        for (int i = b; i < e; i++) {
-            const Q4<T> ig = ldq(m.igeo, i);
-            const T dx = ig.p[2], dy = ig.p[3];
+        if constexpr (sizeof(T) == 8) {
+            // FP64: only about 5 % of the (incidence, component) checks bound the face value and
+            // need a quotient, but a conditional IEEE division is if-converted (computed for every
+            // check).  So one pass flags the checks that need one (bit 4*(incidence - i0) + component,
+            // 16 incidences per word) and a second loop takes one flagged check per trip - one
+            // division per trip, so a warp runs as many divisions as its busiest cell has flags -
+            // in ascending bit order, so every min2 applies in the original sequence per component.
+            // An unflagged check's factor 1 leaves phi unchanged bit for bit (phi <= 1).
+            for (int i0 = b; i0 < e; i0 += 16) {
+                const int i1 = min(e, i0 + 16);
+                unsigned long long mask = 0;
+                for (int i = i0; i < i1; i++) {
+                    const Q4<T> ig = ldq(m.igeo, i);
 #pragma unroll
-            for (int j = 0; j < 4; j++) {
-                const T qf = first_stage ? T(-101) : qp.p[j] + gpx.p[j] * dx + gpy.p[j] * dy;
-                T ph = T(1);
-                if (less(qf, qmin[j])) ph = (qmin[j] - qc.p[j]) / (qf - qc.p[j]);
-                else if (less(qmax[j], qf)) ph = (qmax[j] - qc.p[j]) / (qf - qc.p[j]);
-                phi[j] = min2(ph, phi[j]);
+                    for (int j = 0; j < 4; j++) {
+                        const T qf = first_stage ? T(-101) : qp.p[j] + gpx.p[j] * ig.p[2] + gpy.p[j] * ig.p[3];
+                        if (less(qf, qmin[j]) || less(qmax[j], qf)) mask |= 1ull << (4 * (i - i0) + j);
+                    }
+                }
+                while (mask) {
+                    const int bit = __ffsll((long long)mask) - 1;
+                    mask &= mask - 1;
+                    const int j = bit & 3;
+                    const Q4<T> ig = ldq(m.igeo, i0 + (bit >> 2));
+                    const T qpj = pick4(qp.p, j), gxj = pick4(gpx.p, j), gyj = pick4(gpy.p, j);
+                    const T qcj = pick4(qc.p, j), mn = pick4(qmin, j), mx = pick4(qmax, j);
+                    const T qf = first_stage ? T(-101) : qpj + gxj * ig.p[2] + gyj * ig.p[3];
+                    const T num = less(qf, mn) ? mn : mx;
+                    const T ph = min2((num - qcj) / (qf - qcj), pick4(phi, j));
+#pragma unroll
+                    for (int jj = 0; jj < 4; jj++) phi[jj] = jj == j ? ph : phi[jj];
+                }
+            }
+        } else {
+            for (int i = b; i < e; i++) {
+                const Q4<T> ig = ldq(m.igeo, i);
+                const T dx = ig.p[2], dy = ig.p[3];
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const T qf = first_stage ? T(-101) : qp.p[j] + gpx.p[j] * dx + gpy.p[j] * dy;
+                    T ph = T(1);
+                    if (less(qf, qmin[j])) ph = (qmin[j] - qc.p[j]) / (qf - qc.p[j]);
+                    else if (less(qmax[j], qf)) ph = (qmax[j] - qc.p[j]) / (qf - qc.p[j]);
+                    phi[j] = min2(ph, phi[j]);
+                }
             }
         }
 #pragma unroll
