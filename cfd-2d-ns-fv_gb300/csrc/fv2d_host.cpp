@@ -339,6 +339,18 @@ void renumber(HostMesh& m) {
         key[c] = ((uint64_t)(spread16(ix) | (spread16(iy) << 1)) << 32) | (uint32_t)c;
     }
     std::sort(key.begin(), key.end());
+    // Within each run of kSideBlock Morton-consecutive cells (a small spatial patch), cells are
+    // ordered by face count (stable): a warp's cells then loop over the same number of faces, so
+    // the per-cell gathers do not wait for the warp's one many-sided cell.  Results do not depend
+    // on the order (every per-cell sum runs in ascending original face id).
+    constexpr int kSideBlock = 256;
+    for (int b0 = 0; b0 < nc; b0 += kSideBlock) {
+        const int b1 = std::min(nc, b0 + kSideBlock);
+        std::stable_sort(key.begin() + b0, key.begin() + b1, [&](uint64_t a, uint64_t b) {
+            const int ca = (int)(a & 0xFFFFFFFFu), cb = (int)(b & 0xFFFFFFFFu);
+            return m.cf_off[ca + 1] - m.cf_off[ca] < m.cf_off[cb + 1] - m.cf_off[cb];
+        });
+    }
     m.cell_new2old.resize(nc);
     m.cell_old2new.resize(nc);
     for (int i = 0; i < nc; i++) {

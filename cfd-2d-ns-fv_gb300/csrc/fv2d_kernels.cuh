@@ -91,7 +91,8 @@ __device__ __forceinline__ void prims(const T p[4], const Consts<T>& k, T& rho, 
 // q1 = q0 + RN(a - b*q0)*y brings it within 1 ulp, and with that faithful q1 the residual
 // a - b*q1 is exact and q2 = RN(q1 + (a - b*q1)*y) is the correctly rounded a/b.  Valid for
 // normal operands whose quotient neither overflows nor underflows (all solver quantities); a zero
-// numerator returns the exact signed zero a*y.  Tested bit for bit against IEEE division.
+// numerator (checked on its bits, not with an FP64 compare) returns the exact signed zero a*y.
+// Tested bit for bit against IEEE division.
 // FP32 divides directly (the FP32 engine is built with approximate division).
 template <class T>
 struct Recip {
@@ -103,7 +104,7 @@ struct Recip<double> {
     static __device__ __forceinline__ double of(double b) { return __drcp_rn(b); }
     static __device__ __forceinline__ double div(double a, double b, double y) {
         const double q0 = a * y;
-        if (a == 0.0) return q0;
+        if ((__double_as_longlong(a) << 1) == 0) return q0;   // a == +-0, tested on the integer pipe
         const double q1 = __fma_rn(__fma_rn(-b, q0, a), y, q0);
         return __fma_rn(__fma_rn(-b, q1, a), y, q1);
     }

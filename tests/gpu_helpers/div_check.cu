@@ -15,8 +15,10 @@ __device__ __forceinline__ double rand_double(uint64_t r, uint64_t s, int elo, i
     uint64_t man = r & 0xFFFFFFFFFFFFFULL;
     if (mode == 1) man |= 0xFFFFFFFFFFF00ULL;          // mantissa near all ones
     if (mode == 2) man &= 0x00000000000FFULL;          // mantissa near zero (value near a power of two)
+    // mode 3: a signed zero
     const int e = elo + (int)(s % (uint64_t)(ehi - elo + 1));
     const uint64_t sign = (s >> 40) & 1ULL;
+    if (mode == 3) return __longlong_as_double((long long)(sign << 63));   // +0 or -0
     return __longlong_as_double((long long)((sign << 63) | ((uint64_t)(e + 1023) << 52) | man));
 }
 

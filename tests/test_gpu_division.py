@@ -1,6 +1,6 @@
 """The FP64 engine's shared-reciprocal division (two Markstein corrections) must round exactly
 like IEEE division: checked bit for bit on device-generated operands, including mantissas near
-all-ones / near powers of two and signed operands."""
+all-ones / near powers of two, signed operands and signed-zero dividends."""
 import ctypes
 import os
 import shutil
@@ -39,6 +39,7 @@ def helper(tmp_path_factory, pkg):
     (-30, 30, 0, 2),      # divisor near a power of two
     (-20, 20, 1, 2),
     (-3, 20, 0, 0),       # the solver's range (densities, momenta, energies, volumes)
+    (-30, 30, 3, 0),      # signed-zero dividend: +-0 / b keeps the sign rule of IEEE division
 ])
 def test_shared_reciprocal_division_is_correctly_rounded(helper, elo, ehi, ma, mb):
     bad = ctypes.c_ulonglong()
