@@ -77,6 +77,12 @@ def test_fp64_polygonal_cells_vs_oracle(opts, pkg, orc):
         port.stage()
         assert bits_equal(gpu.get(2), port.get(orc.RES)), f"stage {s}: residual"
         assert bits_equal(gpu.get(0), port.get(orc.QBAR)), f"stage {s}: Qbar"
+        # the gradient kernel's own output (limited LSQ gradient of this stage's input) and dt
+        if s % 3 == 0:
+            assert bits_equal(gpu.get(4), port.get(orc.QBAR_GRAD)), f"stage {s}: Qbar gradient"
+        else:
+            assert bits_equal(gpu.get(5), port.get(orc.QSTAR_GRAD)), f"stage {s}: Q* gradient"
+        assert bits_equal(gpu.get(3), port.get(orc.DT)), f"stage {s}: dt"
     gpu.close()
 
 
