@@ -525,7 +525,8 @@ public:
         if (Qlo_) FV2D_B(cudaMemcpy(lo.data(), Qlo_ + r.c0, sizeof(Q4<T>) * r.n, cudaMemcpyDeviceToHost));
         for (long long c = 0; c < r.n; c++) {
             const int o = r.n2o[c];
-            for (int j = 0; j < 4; j++) q[(size_t)j * r.n + o] = (double)h[c].p[j] + (Qlo_ ? (double)lo[c].p[j] : 0.0);
+            for (int j = 0; j < 4; j++)   // FP64: the value itself (adding 0.0 would turn -0 into +0)
+                q[(size_t)j * r.n + o] = Qlo_ ? (double)h[c].p[j] + (double)lo[c].p[j] : (double)h[c].p[j];
         }
         int f = 0;
         FV2D_B(cudaMemcpy(&f, flags_ + sid, 4, cudaMemcpyDeviceToHost));

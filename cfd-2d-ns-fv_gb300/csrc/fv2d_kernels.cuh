@@ -702,7 +702,8 @@ __global__ void k_state_out(int nc, int ncomp, const int* __restrict__ new2old, 
         Q4<T> lo;
         if (Qlo) lo = Qlo[c];
 #pragma unroll
-        for (int j = 0; j < 4; j++) q[(size_t)(4 * h + j) * nc + o] = (double)v.p[j] + (Qlo ? (double)lo.p[j] : 0.0);
+        // FP64 (no compensation term): the value itself - adding 0.0 would turn -0 into +0
+        for (int j = 0; j < 4; j++) q[(size_t)(4 * h + j) * nc + o] = Qlo ? (double)v.p[j] + (double)lo.p[j] : (double)v.p[j];
     }
 }
 
