@@ -451,8 +451,11 @@ __device__ __forceinline__ void face_flux(int f, const DevMesh<T>& m, const Q4<T
     if (LAST) sout[f] = (fabs(vna) + ca) * A;
 }
 
+#ifndef FV2D_KF_MINB32
+#define FV2D_KF_MINB32 5   // 48 registers (16 B spill): 11 % faster than 4 blocks at 63 registers
+#endif
 template <class T, bool ORDER2, bool NS, bool LAST>
-__global__ void __launch_bounds__(kStageBlock<T>, sizeof(T) == 4 ? 4 : FV2D_FP64_FMINB)
+__global__ void __launch_bounds__(kStageBlock<T>, sizeof(T) == 4 ? FV2D_KF_MINB32 : FV2D_FP64_FMINB)
 k_face(int nf, DevMesh<T> m, const Q4<T>* __restrict__ Q, const Q4<T>* __restrict__ G, Q4<T>* __restrict__ tout,
        T* __restrict__ sout, Consts<T> k, int init_prims) {
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
