@@ -10,7 +10,7 @@ from __future__ import annotations
 
 import time
 
-BLOCKS = (128, 256, 512)
+BLOCKS = (128, 256)             # the batch kernels accept blocks up to 256 threads
 MULTS = (1, 2, 4, 8)
 
 

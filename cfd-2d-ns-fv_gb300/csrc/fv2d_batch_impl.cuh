@@ -63,16 +63,19 @@ __device__ __forceinline__ T block_max_t(T v, T* red) {
     return s;   // valid in thread 0
 }
 
-// Largest block the batch kernels accept (the autotuner's largest) and the FP32 gradient's
-// minimum resident blocks at that size (its register cap).
+// Largest block the batch kernels accept (the autotuner's largest) and the FP32 kernels' minimum
+// resident blocks at that size (their register caps: gradient 64, face 48 - measured fastest);
+// FP64 keeps a 128-register cap.
 #ifndef FV2D_KB_MAXT
-#define FV2D_KB_MAXT 512
+#define FV2D_KB_MAXT 256
 #endif
 #ifndef FV2D_KBG_MINB32
-#define FV2D_KBG_MINB32 2
+#define FV2D_KBG_MINB32 4
 #endif
+constexpr int kBatchMaxBlock = FV2D_KB_MAXT;
+constexpr int kBatchMinB64 = 512 / FV2D_KB_MAXT;
 template <class T>
-__global__ void __launch_bounds__(FV2D_KB_MAXT, sizeof(T) == 4 ? FV2D_KBG_MINB32 : 1)
+__global__ void __launch_bounds__(FV2D_KB_MAXT, sizeof(T) == 4 ? FV2D_KBG_MINB32 : kBatchMinB64)
 kb_gradient(const Tile* __restrict__ tiles, const int* __restrict__ ntiles, DevMesh<T> m,
             const SolveParams<T>* __restrict__ P, const Q4<T>* __restrict__ Qin, const Q4<T>* __restrict__ Qprev,
             const Q4<T>* __restrict__ Gprev, Q4<T>* __restrict__ Gout) {
@@ -95,8 +98,11 @@ kb_gradient(const Tile* __restrict__ tiles, const int* __restrict__ ntiles, DevM
     }
 }
 
+#ifndef FV2D_KBF_MINB32
+#define FV2D_KBF_MINB32 5
+#endif
 template <class T, bool LAST>
-__global__ void __launch_bounds__(FV2D_KB_MAXT, sizeof(T) == 4 ? 2 : 1)
+__global__ void __launch_bounds__(FV2D_KB_MAXT, sizeof(T) == 4 ? FV2D_KBF_MINB32 : kBatchMinB64)
 kb_face(const Tile* __restrict__ tiles, const int* __restrict__ ntiles, DevMesh<T> m,
         const SolveParams<T>* __restrict__ P, const Q4<T>* __restrict__ Qin, const Q4<T>* __restrict__ G,
         Q4<T>* __restrict__ tout, T* __restrict__ sout) {
@@ -540,7 +546,10 @@ public:
     }
 
     int set_tuning(const BatchTuning& t) override {
-        if (t.block < 64 || t.block > 512 || (t.block & 31)) { err_ = "block must be a multiple of 32 in [64, 512]"; return FV2D_ERR_ARG; }
+        if (t.block < 64 || t.block > kBatchMaxBlock || (t.block & 31)) {
+            err_ = "block must be a multiple of 32 in [64, " + std::to_string(kBatchMaxBlock) + "]";
+            return FV2D_ERR_ARG;
+        }
         for (int b = 0; b < 3; b++) if (t.tile_mult[b] < 1 || t.tile_mult[b] > 64) { err_ = "tile multiple out of range"; return FV2D_ERR_ARG; }
         FV2D_B(cudaStreamSynchronize(stream_));
         tune_ = t;

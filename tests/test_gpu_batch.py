@@ -78,7 +78,7 @@ def test_batch_join_and_leave(pkg):
 def test_batch_tuning_does_not_change_results(pkg):
     cases = mix(pkg)[:2]
     results = []
-    for block, mult in ((256, (1, 2, 4)), (128, (1, 1, 1)), (512, (4, 8, 2))):
+    for block, mult in ((256, (1, 2, 4)), (128, (1, 1, 1)), (256, (4, 8, 2))):
         b = pkg.Batch(100000, 300000, 4, precision=pkg.FP64)
         b.set_tuning(block, mult, (4000, 8000))
         ids = [b.add(g, c) for g, c in cases]
