@@ -14,6 +14,7 @@ import os
 import shutil
 import subprocess
 
+import numpy as np
 import pytest
 
 import cli_check
@@ -106,3 +107,28 @@ def test_host_code_clean_under_asan_ubsan(oracle_cli_sanitized, case, tmp_path):
     writers) has no memory errors or undefined behaviour on the golden cases (ASan + UBSan)."""
     env = dict(os.environ, ASAN_OPTIONS="detect_leaks=0", UBSAN_OPTIONS="print_stacktrace=1")
     assert cli_check.run_case([oracle_cli_sanitized], case, str(tmp_path), env=env) == []
+
+
+@pytest.mark.gpu
+def test_gpu_cli_fp32_tracks_fp64(pkg, tmp_path):
+    """lib/fv2d_gpu --fp32 writes the same files from the FP32 engine; its restart state stays within
+    FP32 round-off of the FP64 run (the restart file's 6 significant digits bound the comparison)."""
+    case = next(c for c in CASES if os.path.basename(c).startswith("ch16_euler_sq_global"))
+    prog = pkg.build.CLI
+    states = {}
+    for flag in ("", "--fp32"):
+        work = tmp_path / (flag.strip("-") or "fp64")
+        argv = [prog] + ([flag] if flag else [])
+        grid_txt, inputs, files = cli_check.load_case(case)
+        os.makedirs(work, exist_ok=True)
+        (work / "grid_file.in").write_text(grid_txt)
+        (work / "input.in").write_text(inputs[0])
+        r = subprocess.run(argv, cwd=work, capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, r.stderr[-500:]
+        got = sorted(f"{s}/{n}" for s in ("sol", "mesh") for n in os.listdir(work / s))
+        assert got == sorted(files)
+        rows = (work / "sol" / "restart_sol.dat").read_text().split("\n")[1:]
+        states[flag] = np.array([[float(x) for x in ln.split()] for ln in rows if ln.strip()])
+    a, b = states[""], states["--fp32"]
+    assert a.shape == b.shape
+    assert np.max(np.abs(b - a) / np.abs(a)) < 2e-5
