@@ -119,6 +119,14 @@ int fv2d_read_grid(const char* path, int* num_points, int* num_faces, int* num_c
 
 void fv2d_free(void* p) { std::free(p); }
 
+int fv2d_write_grid(const char* path, const fv2d_mesh_desc* d) {
+    if (!path || !d || !d->x || !d->y || !d->face_point1 || !d->face_point2 || !d->face_cell1 || !d->face_cell2)
+        return fail(FV2D_ERR_ARG, "null argument");
+    std::string err;
+    const int rc = fv2d::write_grid(path, d, err);
+    return rc ? fail(rc, err) : FV2D_OK;
+}
+
 int fv2d_mesh_build(const fv2d_mesh_desc* desc, const fv2d_case* cs, fv2d_mesh** out) {
     if (!out) return fail(FV2D_ERR_ARG, "null output");
     *out = nullptr;

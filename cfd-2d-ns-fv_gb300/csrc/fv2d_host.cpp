@@ -145,6 +145,37 @@ int parse_grid(const char* path, std::vector<double>& x, std::vector<double>& y,
     return FV2D_OK;
 }
 
+int write_grid(const char* path, const fv2d_mesh_desc* d, std::string& err) {
+    FILE* fh = std::fopen(path, "wb");
+    if (!fh) { err = std::string("cannot write grid file ") + path; return FV2D_ERR_IO; }
+    std::vector<char> buf(size_t(1) << 22);
+    size_t used = 0;
+    bool ok = true;
+    auto flush = [&]() {
+        if (used && std::fwrite(buf.data(), 1, used, fh) != used) ok = false;
+        used = 0;
+    };
+    auto room = [&](size_t n) { if (used + n > buf.size()) flush(); };
+    room(64);
+    used += (size_t)std::snprintf(buf.data() + used, 64, "%d %d %d\n", d->num_points, d->num_faces, d->num_cells);
+    for (int i = 0; i < d->num_points; i++) {   // 17 significant digits: every double round-trips
+        room(64);
+        used += (size_t)std::snprintf(buf.data() + used, 64, "%.17g %.17g\n", d->x[i], d->y[i]);
+    }
+    for (int f = 0; f < d->num_faces; f++) {
+        room(32);
+        used += (size_t)std::snprintf(buf.data() + used, 32, "%d %d\n", d->face_point1[f], d->face_point2[f]);
+    }
+    for (int f = 0; f < d->num_faces; f++) {
+        room(32);
+        used += (size_t)std::snprintf(buf.data() + used, 32, "%d %d\n", d->face_cell1[f], d->face_cell2[f]);
+    }
+    flush();
+    if (std::fclose(fh) != 0) ok = false;
+    if (!ok) { err = std::string("write failed: ") + path; return FV2D_ERR_IO; }
+    return FV2D_OK;
+}
+
 // ------------------------------------------------------------------------------------ mesh build
 namespace {
 

@@ -54,6 +54,7 @@ int parse_inputs(const char* path, fv2d_case* cs, std::string& err);
 int parse_grid(const char* path, std::vector<double>& x, std::vector<double>& y,
                std::vector<int>& fp1, std::vector<int>& fp2, std::vector<int>& fc1,
                std::vector<int>& fc2, int& nc, std::string& err);
+int write_grid(const char* path, const fv2d_mesh_desc* d, std::string& err);
 int build_mesh(const fv2d_mesh_desc* d, const fv2d_case* cs, HostMesh& m, std::string& err);
 void build_layout(const HostMesh& m, DeviceLayout& L);
 int mesh_field(const HostMesh& m, int field, double* out);

@@ -24,7 +24,7 @@ GEOM = dict(area=20, nx=21, ny=22, fcx=23, fcy=24, c1dx=25, c1dy=26, c2dx=27, c2
             lx=32, ly=33, mx=34, my=35, vol=40, ccx=41, ccy=42, Ixx=43, Iyy=44, Ixy=45, delta=46, bccx=50, bccy=51)
 BC = {"FREESTREAM": -1, "SLIP_WALL": -2, "EXTRAPOLATION": -3, "NO_SLIP_WALL": -4}
 EXPORTS = [
-    "fv2d_read_inputs", "fv2d_read_grid", "fv2d_free", "fv2d_mesh_build", "fv2d_mesh_free", "fv2d_mesh_sizes",
+    "fv2d_read_inputs", "fv2d_read_grid", "fv2d_write_grid", "fv2d_free", "fv2d_mesh_build", "fv2d_mesh_free", "fv2d_mesh_sizes",
     "fv2d_mesh_get", "fv2d_mesh_permutation", "fv2d_create", "fv2d_create_from_files", "fv2d_destroy",
     "fv2d_step", "fv2d_stage", "fv2d_set_state", "fv2d_load_state", "fv2d_get_state", "fv2d_get_field", "fv2d_residual_norm",
     "fv2d_sizes", "fv2d_save", "fv2d_post", "fv2d_write_history_headers", "fv2d_write_mesh_files",
@@ -77,6 +77,9 @@ def library():
         sig = {
             "fv2d_read_inputs": (ctypes.c_int, [cp, ctypes.POINTER(Case)]),
             "fv2d_free": (None, [vp]),
+            "fv2d_read_grid": (ctypes.c_int, [cp, ip, ip, ip, ctypes.POINTER(dp), ctypes.POINTER(dp), ctypes.POINTER(ip),
+                                              ctypes.POINTER(ip), ctypes.POINTER(ip), ctypes.POINTER(ip)]),
+            "fv2d_write_grid": (ctypes.c_int, [cp, ctypes.POINTER(MeshDesc)]),
             "fv2d_mesh_build": (ctypes.c_int, [ctypes.POINTER(MeshDesc), ctypes.POINTER(Case), pvp]),
             "fv2d_mesh_free": (None, [vp]),
             "fv2d_mesh_sizes": (ctypes.c_int, [vp, ip]),
@@ -151,6 +154,32 @@ def read_inputs(path: str) -> Case:
     cs = Case()
     _check(library().fv2d_read_inputs(path.encode(), ctypes.byref(cs)))
     return cs
+
+
+def read_grid(path: str):
+    """Parse a grid_file.in (C++ parser): (x, y, face_point1, face_point2, face_cell1, face_cell2,
+    num_cells), ids 1-based as in the file."""
+    lib = library()
+    npt, nf, nc = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    px, py = ctypes.POINTER(ctypes.c_double)(), ctypes.POINTER(ctypes.c_double)()
+    pi = [ctypes.POINTER(ctypes.c_int)() for _ in range(4)]
+    _check(lib.fv2d_read_grid(path.encode(), ctypes.byref(npt), ctypes.byref(nf), ctypes.byref(nc), ctypes.byref(px),
+                              ctypes.byref(py), *[ctypes.byref(p) for p in pi]))
+    try:
+        x = np.ctypeslib.as_array(px, shape=(npt.value,)).copy()
+        y = np.ctypeslib.as_array(py, shape=(npt.value,)).copy()
+        ids = [np.ctypeslib.as_array(p, shape=(nf.value,)).copy() for p in pi]
+    finally:
+        for p in [px, py] + pi:
+            lib.fv2d_free(ctypes.cast(p, ctypes.c_void_p))
+    return (x, y, *ids, nc.value)
+
+
+def write_grid(path: str, grid):
+    """Write `grid` (x, y, fp1, fp2, fc1, fc2 1-based, num_cells) as a grid_file.in (C++ writer,
+    17 significant digits)."""
+    d = _Desc(grid)
+    _check(library().fv2d_write_grid(path.encode(), ctypes.byref(d.desc)))
 
 
 def read_restart(path: str, num_cells: int):

@@ -91,6 +91,9 @@ int fv2d_read_grid(const char* path, int* num_points, int* num_faces, int* num_c
                    double** x, double** y, int** face_point1, int** face_point2,
                    int** face_cell1, int** face_cell2);
 void fv2d_free(void* p);
+/* Write a mesh in the grid_file.in format readmesh() reads (src/base/readmesh.cpp:31-70); point
+ * coordinates with 17 significant digits, so fv2d_read_grid returns the same doubles.  Host only. */
+int fv2d_write_grid(const char* path, const fv2d_mesh_desc* desc);
 
 /* Host mesh build: connectivity, BC tagging and geometry exactly as readmesh()
  * (src/base/readmesh.cpp:31-411), plus the cell/face renumbering used on the device.          */
