@@ -123,7 +123,7 @@ def bytes_per_launch(kernel, N, F, ninc, Nb, s, ns, squeeze, comp=False, store_r
         b += Nb * 2 * s                          # nx, ny on boundary faces
         return b
     if kernel in ("k_face", "kb_face"):
-        geo = 9 + (5 if (ns and order2) else 0)
+        geo = 7 + (3 if (ns and order2) else 0)  # nx ny area c1dx c1dy c2dx c2dy [+ lx ly dist]
         b = F * (8 + geo * s)                    # c1, c2, geometry
         b += N * (4 * s + (8 * s if order2 else 0))   # Q (and G) of every cell
         b += F * 4 * s                           # t written
