@@ -389,9 +389,11 @@ void renumber(HostMesh& m) {
         m.cell_new2old[i] = c;
         m.cell_old2new[c] = i;
     }
-    // faces follow their first cell in the new order (ties by original id)
+    // faces follow their first cell in the new order (ties by original id); boundary faces go after
+    // all interior faces, so the face kernel's warps do not mix the boundary and interior branches
     std::vector<uint64_t> fk(nf);
-    for (int f = 0; f < nf; f++) fk[f] = ((uint64_t)m.cell_old2new[m.fc1[f]] << 32) | (uint32_t)f;
+    for (int f = 0; f < nf; f++)
+        fk[f] = ((uint64_t)(m.fc2[f] < 0 ? 1 : 0) << 63) | ((uint64_t)m.cell_old2new[m.fc1[f]] << 32) | (uint32_t)f;
     std::sort(fk.begin(), fk.end());
     m.face_new2old.resize(nf);
     m.face_old2new.resize(nf);
