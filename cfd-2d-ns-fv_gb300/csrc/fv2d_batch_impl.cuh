@@ -282,6 +282,7 @@ public:
         for (int i = 0; i < 3; i++) oq[i] = take(q4 * Nc_);
         for (int i = 0; i < 3; i++) og[i] = take(2 * q4 * Nc_);
         size_t odt = take(sizeof(T) * Nc_), oS = take(sizeof(T) * Nc_), ovol = take(sizeof(T) * Nc_);
+        size_t orvol = take(sizeof(T) * Nc_), ordist = take(sizeof(T) * Fc_);
         size_t oixx = take(8 * Nc_), oiyy = take(8 * Nc_), oixy = take(8 * Nc_), ooff = take(4 * Nc_);
         size_t oinc = take(4 * Ic_), onbr = take(4 * Ic_), oigeo = take(q4 * Ic_);
         size_t ofc1 = take(4 * Fc_), ofc2 = take(4 * Fc_), oqc = take(4 * Fc_);
@@ -315,6 +316,7 @@ public:
         m_.g.c2dx = geo_[5]; m_.g.c2dy = geo_[6]; m_.g.dxj = geo_[7]; m_.g.dyj = geo_[8]; m_.g.mx = geo_[9];
         m_.g.my = geo_[10]; m_.g.lx = geo_[11]; m_.g.ly = geo_[12]; m_.g.dist = geo_[13];
         m_.Ixx = ixx; m_.Iyy = iyy; m_.Ixy = ixy; m_.vol = vol;
+        m_.rvol = (T*)(a + orvol); m_.rdist = (T*)(a + ordist);
         FV2D_B(cudaMemsetAsync(arena_, 0, bytes_, stream_));
         FV2D_B(cudaStreamSynchronize(stream_));
         cells_.reset(Nc_);
@@ -418,6 +420,13 @@ public:
         FV2D_B(up(m_.vol + r.c0, im->o_vol, sizeof(T) * n));
         FV2D_B(up(m_.igeo + r.i0, im->o_igeo, sizeof(T) * 4 * k));
         for (int gI = 0; gI < 14; gI++) FV2D_B(up(geo_[gI] + r.f0, im->o_geo[gI], sizeof(T) * m));
+        {   // geometry reciprocals of the solve's ranges
+            const long long mx = std::max<long long>(r.n, r.m);
+            const int gr = (int)std::min<long long>((mx + 255) / 256, 4LL * sms_);
+            k_reciprocals<T><<<gr, 256, 0, stream_>>>((int)r.m, geo_[13] + r.f0, (T*)m_.rdist + r.f0, (int)r.n,
+                                                    m_.vol + r.c0, (T*)m_.rvol + r.c0);
+            FV2D_B(cudaGetLastError());
+        }
         // solve-local ids -> arena ids, on the device
         {
             const long long mx = std::max<long long>({r.n + 1, r.k, r.m});

@@ -45,6 +45,9 @@ struct DevMesh {
     FaceGeo<T> g;
     const double *Ixx, *Iyy, *Ixy;
     const T* vol;
+    // geometry-only reciprocals, computed once (k_reciprocals) with the same Recip<T>::of the kernels
+    // would evaluate every stage: 1/|dist| per face (NS interior faces), 1/vol per cell
+    const T *rdist, *rvol;
 };
 
 template <class T>
@@ -394,7 +397,7 @@ __device__ __forceinline__ void face_flux(int f, const DevMesh<T>& m, const Q4<T
         bool have = true;
         if (c2 >= 0) {
             const T ad = fabs(g.dist[f]);
-            const T yd = Recip<T>::of(ad);
+            const T yd = m.rdist[f];   // Recip<T>::of(ad), precomputed
             // unit tangent p1 -> p2 (readmesh.cpp:400-406) from the normal: mx = dx/|d| = -ny and
             // my = dy/|d| = nx, bit for bit (same |d| expression, sign-symmetric rounding)
             const T mxf = -fny, myf = fnx, lxf = g.lx[f], lyf = g.ly[f];
@@ -585,7 +588,7 @@ __device__ __forceinline__ T update_cell(int c, const DevMesh<T>& m, const Q4<T>
         }
     }
     const T vc = m.vol[c];
-    const T yv = Recip<T>::of(vc);
+    const T yv = m.rvol[c];   // Recip<T>::of(vc), precomputed
 #pragma unroll
     for (int j = 0; j < 4; j++) r[j] = Recip<T>::div(r[j], vc, yv);
     if (Rout) { Q4<T> rr; for (int j = 0; j < 4; j++) rr.p[j] = r[j]; Rout[c] = rr; }
@@ -670,6 +673,17 @@ k_update(int nc, DevMesh<T> m, const Q4<T>* __restrict__ tface, const T* __restr
     if (STAGE == 2) {
         const T mx = block_max(c < nc ? snext : T(0));
         if (threadIdx.x == 0) atomic_max_pos(smax, mx);
+    }
+}
+
+// Geometry-only reciprocals of a mesh (or of one solve's ranges in a batch arena): rdist = 1/|dist|
+// (dist may be null: no NS faces) and rvol = 1/vol, with the kernels' own Recip<T>::of.
+template <class T>
+__global__ void k_reciprocals(int nf, const T* __restrict__ dist, T* __restrict__ rdist, int nc,
+                              const T* __restrict__ vol, T* __restrict__ rvol) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < max(nf, nc); i += gridDim.x * blockDim.x) {
+        if (i < nf && dist) rdist[i] = Recip<T>::of(fabs(dist[i]));
+        if (i < nc) rvol[i] = Recip<T>::of(vol[i]);
     }
 }
 

@@ -69,6 +69,7 @@ public:
         for (int i = 0; i < 3; i++) o_g[i] = take(2 * q4 * nc_);
         size_t o_r = take(q4 * nc_), o_dt = take(sizeof(T) * nc_), o_S = take(sizeof(T) * nc_);
         size_t o_vol = take(sizeof(T) * nc_), o_ixx = take(8 * nc_), o_iyy = take(8 * nc_), o_ixy = take(8 * nc_);
+        size_t o_rvol = take(sizeof(T) * nc_), o_rdist = take(sizeof(T) * nf_);
         size_t o_incoff = take(4 * (nc_ + 1)), o_inc = take(4 * (size_t)ninc_), o_nbr = take(4 * (size_t)ninc_);
         size_t o_igeo = take(q4 * (size_t)ninc_);
         size_t o_fc1 = take(4 * (size_t)nf_), o_fc2 = take(4 * (size_t)nf_), o_qcell = take(4 * (size_t)nf_);
@@ -99,6 +100,7 @@ public:
         dm_.inc_off = inc_off_; dm_.inc = inc_; dm_.nbr = nbr_; dm_.fc1 = fc1_; dm_.fc2 = fc2_; dm_.qcell = qcell_;
         dm_.igeo = (const Q4<T>*)(a + o_igeo);
         dm_.g = g_; dm_.Ixx = Ixx_; dm_.Iyy = Iyy_; dm_.Ixy = Ixy_; dm_.vol = vol_;
+        dm_.rvol = (T*)(a + o_rvol); dm_.rdist = (T*)(a + o_rdist);
         smax_ = (T*)(a + o_smax); flag_ = (int*)(a + o_flag);
         n2o_ = (int*)(a + o_n2o); dstage_ = (double*)(a + o_stage); part_ = (double*)(a + o_part);
         D_ = comp ? (Q4<T>*)(a + o_D) : nullptr;
@@ -139,6 +141,11 @@ public:
             const size_t n0 = std::min(L.igeo.size() - i0, staging_bytes_ / sizeof(T));
             std::vector<double> part(L.igeo.begin() + i0, L.igeo.begin() + i0 + n0);
             if ((rc = putT((T*)(a + o_igeo) + i0, part))) return rc;
+        }
+        {
+            const int mx = std::max(nf_, nc_);
+            k_reciprocals<T><<<(mx + 255) / 256, 256, 0, stream_>>>(nf_, g_.dist, (T*)dm_.rdist, nc_, vol_, (T*)dm_.rvol);
+            FV2D_CUDA(cudaGetLastError());
         }
         return reset_freestream();
     }
