@@ -113,15 +113,19 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def bytes_per_launch(kernel, N, F, ninc, Nb, s, ns, squeeze, comp=False, store_r=True, order2=True):
+def bytes_per_launch(kernel, N, F, ninc, Nb, s, ns, squeeze, comp=False, store_r=True, order2=True, fval=False):
     """Algorithmic bytes of one launch (average over the three RK stages): every array element the
     kernel must touch, counted once.  s = state bytes (8 FP64, 4 FP32); ids 4 B; LSQ moments 8 B.
-    comp: FP32 delta-form increments and compensated base state; store_r: residual kept (last stage)."""
+    comp: FP32 delta-form increments and compensated base state; store_r: residual kept (last stage);
+    fval: the face pass stores its reconstructed face states and the squeeze reads them (FP64 single
+    solve) instead of recomputing them from the previous stage's Q and limited G."""
     if kernel in ("k_gradient", "kb_gradient"):
         if not order2:
             return 0.0
         b = N * (4 * s + 8 * s)                  # Q read, G write
-        if squeeze:
+        if squeeze and fval:
+            b += ninc * 4 * s                    # stored face state on the cell's side, per incidence
+        elif squeeze:
             b += N * (4 * s + 8 * s)             # previous Q and limited G
         b += N * 4 + ninc * 8 + N * 24           # CSR offsets, (face, neighbour) pairs, Ixx/Iyy/Ixy
         b += ninc * 4 * s                        # per-incidence dxj, dyj, face-centre offset
@@ -133,6 +137,8 @@ def bytes_per_launch(kernel, N, F, ninc, Nb, s, ns, squeeze, comp=False, store_r
         b += N * (4 * s + (8 * s if order2 else 0))   # Q (and G) of every cell
         b += F * 4 * s                           # t written
         b += (F * s) / 3.0                       # spectral term, last stage only
+        if squeeze and fval and order2:
+            b += (2 * F - Nb) * 4 * s            # face states stored for the next squeeze
         return b
     if kernel in ("k_update", "kb_update"):
         b = N * 4 + ninc * 4 + F * 4 * s         # CSR, face contributions
@@ -295,7 +301,7 @@ def run_reference_arm(args):
 
 
 def single_kernel_bytes(N, F, ninc, Nb, s, comp, store_r=True):
-    return {k: bytes_per_launch(k, N, F, ninc, Nb, s, True, True, comp=comp, store_r=store_r)
+    return {k: bytes_per_launch(k, N, F, ninc, Nb, s, True, True, comp=comp, store_r=store_r, fval=(s == 8))
             for k in ("k_gradient", "k_face", "k_update")}
 
 

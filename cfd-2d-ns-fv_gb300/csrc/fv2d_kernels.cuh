@@ -48,6 +48,11 @@ struct DevMesh {
     // geometry-only reciprocals, computed once (k_reciprocals) with the same Recip<T>::of the kernels
     // would evaluate every stage: 1/|dist| per face (NS interior faces), 1/vol per cell
     const T *rdist, *rvol;
+    // reconstructed face states of the last face pass, [2 nf]: 2f + side (the incidence code) holds
+    // the state on cell c1's (side 0) or c2's (side 1) side of face f - exactly the stale face
+    // values the next squeeze reads.  Null: the squeeze recomputes them from the previous stage's
+    // state and limited gradient with the same expression.
+    Q4<T>* fval;
 };
 
 template <class T>
@@ -229,7 +234,8 @@ __device__ __forceinline__ void gradient_cell(int c, const DevMesh<T>& m, const 
     if (SQUEEZE) {
         T phi[4] = {T(1), T(1), T(1), T(1)};
         Q4<T> qp, gpx, gpy;
-        if (!first_stage) { qp = ldq(Qprev, c); gpx = ldq(Gprev, 2 * c); gpy = ldq(Gprev, 2 * c + 1); }
+        const Q4<T>* __restrict__ fval = m.fval;
+        if (!first_stage && !fval) { qp = ldq(Qprev, c); gpx = ldq(Gprev, 2 * c); gpy = ldq(Gprev, 2 * c + 1); }
         if constexpr (sizeof(T) == 8) {
             // FP64: only about 5 % of the (incidence, component) checks bound the face value and
             // need a quotient, but a conditional IEEE division is if-converted (computed for every
@@ -242,21 +248,33 @@ __device__ __forceinline__ void gradient_cell(int c, const DevMesh<T>& m, const 
                 const int i1 = min(e, i0 + 16);
                 unsigned long long mask = 0;
                 for (int i = i0; i < i1; i++) {
-                    const Q4<T> ig = ldq(m.igeo, i);
+                    Q4<T> qf;
+                    if (first_stage) {
 #pragma unroll
-                    for (int j = 0; j < 4; j++) {
-                        const T qf = first_stage ? T(-101) : qp.p[j] + gpx.p[j] * ig.p[2] + gpy.p[j] * ig.p[3];
-                        if (less(qf, qmin[j]) || less(qmax[j], qf)) mask |= 1ull << (4 * (i - i0) + j);
+                        for (int j = 0; j < 4; j++) qf.p[j] = T(-101);
+                    } else if (fval) {
+                        qf = ldq(fval, inc[i]);
+                    } else {
+                        const Q4<T> ig = ldq(m.igeo, i);
+#pragma unroll
+                        for (int j = 0; j < 4; j++) qf.p[j] = qp.p[j] + gpx.p[j] * ig.p[2] + gpy.p[j] * ig.p[3];
                     }
+#pragma unroll
+                    for (int j = 0; j < 4; j++)
+                        if (less(qf.p[j], qmin[j]) || less(qmax[j], qf.p[j])) mask |= 1ull << (4 * (i - i0) + j);
                 }
                 while (mask) {
                     const int bit = __ffsll((long long)mask) - 1;
                     mask &= mask - 1;
-                    const int j = bit & 3;
-                    const Q4<T> ig = ldq(m.igeo, i0 + (bit >> 2));
-                    const T qpj = pick4(qp.p, j), gxj = pick4(gpx.p, j), gyj = pick4(gpy.p, j);
+                    const int j = bit & 3, i = i0 + (bit >> 2);
                     const T qcj = pick4(qc.p, j), mn = pick4(qmin, j), mx = pick4(qmax, j);
-                    const T qf = first_stage ? T(-101) : qpj + gxj * ig.p[2] + gyj * ig.p[3];
+                    T qf;
+                    if (first_stage) qf = T(-101);
+                    else if (fval) qf = reinterpret_cast<const T*>(fval)[4 * (size_t)inc[i] + j];
+                    else {
+                        const Q4<T> ig = ldq(m.igeo, i);
+                        qf = pick4(qp.p, j) + pick4(gpx.p, j) * ig.p[2] + pick4(gpy.p, j) * ig.p[3];
+                    }
                     const T num = less(qf, mn) ? mn : mx;
                     const T ph = min2((num - qcj) / (qf - qcj), pick4(phi, j));
 #pragma unroll
@@ -368,6 +386,13 @@ __device__ __forceinline__ void face_flux(int f, const DevMesh<T>& m, const Q4<T
         for (int j = 0; j < 4; j++) Rq[j] = L[j];
     } else {
         cons(lrho, -lu, -lv, lP, k, Rq);
+    }
+    if (m.fval) {   // the next squeeze's stale face values (BC faces: the c1 side only)
+        Q4<T> lq, rq;
+#pragma unroll
+        for (int j = 0; j < 4; j++) { lq.p[j] = L[j]; rq.p[j] = Rq[j]; }
+        m.fval[2 * f] = lq;
+        if (c2 >= 0) m.fval[2 * f + 1] = rq;
     }
     T rrho, ru, rv, rP, ry_;
     prims_r(Rq, k, rrho, ru, rv, rP, ry_);

@@ -78,6 +78,10 @@ public:
         size_t o_t = take(q4 * nf_), o_s = take(sizeof(T) * nf_);
         size_t o_smax = take(64), o_flag = take(64);
         size_t o_n2o = take(4 * (size_t)nc_);
+        // FP64 squeeze: the face pass stores its reconstructed states for the next limiter pass
+        // (the FP32 engine, memory-bound, recomputes them instead)
+        const bool store_fval = sizeof(T) == 8 && order2_ && squeeze_;
+        size_t o_fval = store_fval ? take(2 * q4 * (size_t)nf_) : 0;
         size_t o_stage = take(8 * 8 * (size_t)nc_);
         nred_ = 304;
         size_t o_part = take(8 * 4 * (size_t)nred_);
@@ -101,6 +105,7 @@ public:
         dm_.igeo = (const Q4<T>*)(a + o_igeo);
         dm_.g = g_; dm_.Ixx = Ixx_; dm_.Iyy = Iyy_; dm_.Ixy = Ixy_; dm_.vol = vol_;
         dm_.rvol = (T*)(a + o_rvol); dm_.rdist = (T*)(a + o_rdist);
+        dm_.fval = store_fval ? (Q4<T>*)(a + o_fval) : nullptr;
         smax_ = (T*)(a + o_smax); flag_ = (int*)(a + o_flag);
         n2o_ = (int*)(a + o_n2o); dstage_ = (double*)(a + o_stage); part_ = (double*)(a + o_part);
         D_ = comp ? (Q4<T>*)(a + o_D) : nullptr;
