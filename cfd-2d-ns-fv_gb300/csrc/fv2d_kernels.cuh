@@ -151,7 +151,23 @@ __device__ __forceinline__ T pick4(const T a[4], int j) {
     return j == 0 ? a[0] : j == 1 ? a[1] : j == 2 ? a[2] : a[3];
 }
 
-template <class T, bool SQUEEZE>
+#ifndef FV2D_FP64_BLOCK
+#define FV2D_FP64_BLOCK 256   // threads per block of the FP64 gradient and face kernels
+#endif
+
+// Shared-memory staging of the warp-shared limiter quotients (FP64 single solve, see gradient_cell)
+#ifndef FV2D_WARPQ_CAP
+#define FV2D_WARPQ_CAP 256   // flagged checks per warp held at once; warps with more use the per-cell loop
+#endif
+template <int WARPS>
+struct WarpQ {
+    double qc[WARPS][4][32], mn[WARPS][4][32], mx[WARPS][4][32];   // each cell's state and bounds
+    int b[WARPS][32];                                               // each cell's first incidence
+    unsigned short list[WARPS][FV2D_WARPQ_CAP];                     // (lane << 6) | check bit
+    double quo[WARPS][FV2D_WARPQ_CAP];                              // the checks' quotients
+};
+
+template <class T, bool SQUEEZE, bool WARPQ = false>
 __device__ __forceinline__ void gradient_cell(int c, const DevMesh<T>& m, const Q4<T>* __restrict__ Q,
                                               const Q4<T>* __restrict__ Qprev, const Q4<T>* __restrict__ Gprev,
                                               Q4<T>* __restrict__ Gout, const Consts<T>& k, int first_stage,
@@ -244,7 +260,82 @@ __device__ __forceinline__ void gradient_cell(int c, const DevMesh<T>& m, const 
             // division per trip, so a warp runs as many divisions as its busiest cell has flags -
             // in ascending bit order, so every min2 applies in the original sequence per component.
             // An unflagged check's factor 1 leaves phi unchanged bit for bit (phi <= 1).
-            for (int i0 = b; i0 < e; i0 += 16) {
+            // WARPQ (FP64 single solve, stored face states): a warp's flagged checks are listed in
+            // shared memory and spread over its 32 lanes, one quotient per lane per round, so the
+            // warp runs ceil(flagged / 32) divisions instead of its busiest cell's count; each cell
+            // then applies its own quotients in ascending bit order, as the loop below does.
+            bool shared_done = false;
+            if constexpr (WARPQ) {
+                constexpr unsigned FULL = 0xffffffffu;
+                if (fval != nullptr && e - b <= 16 && __activemask() == FULL) {
+                    unsigned long long mask = 0;
+                    for (int i = b; i < e; i++) {
+                        Q4<T> qf;
+                        if (first_stage) {
+#pragma unroll
+                            for (int j = 0; j < 4; j++) qf.p[j] = T(-101);
+                        } else {
+                            qf = ldq(fval, inc[i]);
+                        }
+#pragma unroll
+                        for (int j = 0; j < 4; j++)
+                            if (less(qf.p[j], qmin[j]) || less(qmax[j], qf.p[j])) mask |= 1ull << (4 * (i - b) + j);
+                    }
+                    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+                    const int cnt = __popcll(mask);
+                    int incl = cnt;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int v = __shfl_up_sync(FULL, incl, o);
+                        if (lane >= o) incl += v;
+                    }
+                    const int total = __shfl_sync(FULL, incl, 31), excl = incl - cnt;
+                    if (total <= FV2D_WARPQ_CAP) {
+                        __shared__ WarpQ<FV2D_FP64_BLOCK / 32> sq;
+#pragma unroll
+                        for (int j = 0; j < 4; j++) {
+                            sq.qc[w][j][lane] = qc.p[j];
+                            sq.mn[w][j][lane] = qmin[j];
+                            sq.mx[w][j][lane] = qmax[j];
+                        }
+                        sq.b[w][lane] = b;
+                        {
+                            unsigned long long mm = mask;
+                            int pos = excl;
+                            while (mm) {
+                                const int bit = __ffsll((long long)mm) - 1;
+                                mm &= mm - 1;
+                                sq.list[w][pos++] = (unsigned short)((lane << 6) | bit);
+                            }
+                        }
+                        __syncwarp();
+                        for (int g = lane; g < total; g += 32) {
+                            const int ent = sq.list[w][g], ow = ent >> 6, bit = ent & 63, j = bit & 3;
+                            const T qf = first_stage ? T(-101)
+                                                     : reinterpret_cast<const T*>(fval)[4 * (size_t)inc[sq.b[w][ow] + (bit >> 2)] + j];
+                            const T qcj = sq.qc[w][j][ow], mn = sq.mn[w][j][ow], mx = sq.mx[w][j][ow];
+                            const T num = less(qf, mn) ? mn : mx;
+                            sq.quo[w][g] = (num - qcj) / (qf - qcj);
+                        }
+                        __syncwarp();
+                        {
+                            unsigned long long mm = mask;
+                            int pos = excl;
+                            while (mm) {
+                                const int bit = __ffsll((long long)mm) - 1;
+                                mm &= mm - 1;
+                                const int j = bit & 3;
+                                const T ph = min2((T)sq.quo[w][pos++], pick4(phi, j));
+#pragma unroll
+                                for (int jj = 0; jj < 4; jj++) phi[jj] = jj == j ? ph : phi[jj];
+                            }
+                        }
+                        __syncwarp();
+                        shared_done = true;
+                    }
+                }
+            }
+            for (int i0 = b; i0 < (shared_done ? b : e); i0 += 16) {
                 const int i1 = min(e, i0 + 16);
                 unsigned long long mask = 0;
                 for (int i = i0; i < i1; i++) {
@@ -305,9 +396,6 @@ __device__ __forceinline__ void gradient_cell(int c, const DevMesh<T>& m, const 
 // Occupancy: the FP32 kernels are latency-bound gathers, so their register use is capped for more
 // resident warps.  The FP64 kernels are FP64-pipe-bound; their block size and minimum resident
 // blocks (register cap) set how many warps cover the pipe's latency.
-#ifndef FV2D_FP64_BLOCK
-#define FV2D_FP64_BLOCK 256
-#endif
 #ifndef FV2D_FP64_GMINB
 #define FV2D_FP64_GMINB 2
 #endif
@@ -326,7 +414,7 @@ k_gradient(int nc, DevMesh<T> m, const Q4<T>* __restrict__ Q, const Q4<T>* __res
            const Q4<T>* __restrict__ Gprev, Q4<T>* __restrict__ Gout, Consts<T> k, int first_stage, int init_prims) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= nc) return;
-    gradient_cell<T, SQUEEZE>(c, m, Q, Qprev, Gprev, Gout, k, first_stage, init_prims);
+    gradient_cell<T, SQUEEZE, sizeof(T) == 8>(c, m, Q, Qprev, Gprev, Gout, k, first_stage, init_prims);
 }
 
 // ------------------------------------------------------------------------------------------
