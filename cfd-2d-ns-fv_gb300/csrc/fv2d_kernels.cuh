@@ -250,7 +250,7 @@ __device__ __forceinline__ void gradient_cell(int c, const DevMesh<T>& m, const 
     if (SQUEEZE) {
         T phi[4] = {T(1), T(1), T(1), T(1)};
         Q4<T> qp, gpx, gpy;
-        const Q4<T>* __restrict__ fval = m.fval;
+        const Q4<T>* __restrict__ fval = sizeof(T) == 8 ? m.fval : nullptr;   // FP64 engine only
         if (!first_stage && !fval) { qp = ldq(Qprev, c); gpx = ldq(Gprev, 2 * c); gpy = ldq(Gprev, 2 * c + 1); }
         if constexpr (sizeof(T) == 8) {
             // FP64: only about 5 % of the (incidence, component) checks bound the face value and
@@ -475,12 +475,14 @@ __device__ __forceinline__ void face_flux(int f, const DevMesh<T>& m, const Q4<T
     } else {
         cons(lrho, -lu, -lv, lP, k, Rq);
     }
-    if (m.fval) {   // the next squeeze's stale face values (BC faces: the c1 side only)
-        Q4<T> lq, rq;
+    if constexpr (sizeof(T) == 8) {
+        if (m.fval) {   // the next squeeze's stale face values (BC faces: the c1 side only)
+            Q4<T> lq, rq;
 #pragma unroll
-        for (int j = 0; j < 4; j++) { lq.p[j] = L[j]; rq.p[j] = Rq[j]; }
-        m.fval[2 * f] = lq;
-        if (c2 >= 0) m.fval[2 * f + 1] = rq;
+            for (int j = 0; j < 4; j++) { lq.p[j] = L[j]; rq.p[j] = Rq[j]; }
+            m.fval[2 * f] = lq;
+            if (c2 >= 0) m.fval[2 * f + 1] = rq;
+        }
     }
     T rrho, ru, rv, rP, ry_;
     prims_r(Rq, k, rrho, ru, rv, rP, ry_);
