@@ -118,6 +118,32 @@ struct Recip<double> {
     }
 };
 
+// a/3.  FP64: one residual correction suffices for this divisor (two are needed in general).
+// y = RN(1/3) = 1/3 (1 - 2^-54), so a*y is within half an ulp of a/3 and q0 = RN(a*y) is faithful;
+// r = a - 3 q0 is then exact (an integer multiple of ulp(q0), below 3 ulp), and q0 + r*y is within
+// 2^-53 ulp of a/3.  a/3 lies at least ulp/6 from every rounding midpoint (a - 3m, m a midpoint,
+// is a non-zero multiple of ulp/2), so RN(q0 + r*y) is the correctly rounded a/3.  Checked against
+// IEEE division on the host (tests/cpu_helpers/div3_check.cpp).
+template <class T>
+__device__ __forceinline__ T div3(T a) { return Recip<T>::div(a, T(3), T(1.0 / 3.0)); }
+template <>
+__device__ __forceinline__ double div3<double>(double a) {
+    const double y = 1.0 / 3.0, q0 = a * y;
+    if ((__double_as_longlong(a) << 1) == 0) return q0;   // a == +-0
+    return __fma_rn(__fma_rn(-3.0, q0, a), y, q0);
+}
+
+// +0 - x, IEEE round to nearest, for a term (V A) that is identically +0 (V = +0, area A >= +0):
+// -x, and +0 when x is a zero of either sign
+__device__ __forceinline__ double zero_minus(double x) {
+    const long long b = __double_as_longlong(x) ^ (long long)0x8000000000000000ULL;
+    return (b << 1) == 0 ? 0.0 : __longlong_as_double(b);
+}
+__device__ __forceinline__ float zero_minus(float x) {
+    const int b = __float_as_int(x) ^ (int)0x80000000u;
+    return (b << 1) == 0 ? 0.0f : __int_as_float(b);
+}
+
 // prims() with the reciprocal of rho shared by u, v (and returned for P/rho)
 template <class T>
 __device__ __forceinline__ void prims_r(const T p[4], const Consts<T>& k, T& rho, T& u, T& v, T& P, T& y) {
@@ -547,7 +573,7 @@ __device__ __forceinline__ void face_flux(int f, const DevMesh<T>& m, const Q4<T
         }
         T txx, txy, tyy, dTx, dTy;
         if (have) {
-            const T third = Recip<T>::div(ux + vy, T(3), T(1.0 / 3.0));
+            const T third = div3(ux + vy);
             txx = T(2) * k.mu * (ux - third);
             txy = k.mu * (uy + vx);
             tyy = T(2) * k.mu * (vy - third);
@@ -564,7 +590,11 @@ __device__ __forceinline__ void face_flux(int f, const DevMesh<T>& m, const Q4<T
     }
     Q4<T> t;
 #pragma unroll
-    for (int j = 0; j < 4; j++) t.p[j] = (V[j] * A) - (Fr[j] * A);
+    for (int j = 0; j < 4; j++) {
+        // (V*A) - (F*A); V[0] is always +0, and all of V is +0 for Euler and first order
+        if (j == 0 || !(NS && ORDER2)) t.p[j] = zero_minus(Fr[j] * A);
+        else t.p[j] = (V[j] * A) - (Fr[j] * A);
+    }
     tout[f] = t;
     if (LAST) sout[f] = (fabs(vna) + ca) * A;
 }

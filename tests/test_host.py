@@ -169,6 +169,23 @@ def test_fp64_engine_is_built_without_fma_contraction():
     assert re.search(r'"fv2d_fp64\.cu".*-fmad=false', src)
 
 
+def test_fp64_division_by_three(tmp_path):
+    """The face kernel's FP64 a/3 (one residual correction of RN(a RN(1/3))) equals IEEE a / 3 on
+    random operands of every exponent and on quotients next to rounding midpoints."""
+    import shutil
+    import subprocess
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    exe = str(tmp_path / "div3_check")
+    here = os.path.dirname(os.path.abspath(__file__))
+    subprocess.run([cxx, "-std=c++17", "-O2", "-ffp-contract=off", os.path.join(here, "cpu_helpers", "div3_check.cpp"),
+                    "-o", exe], check=True, capture_output=True)
+    r = subprocess.run([exe, "3000000"], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout
+    assert "0 mismatches" in r.stdout
+
+
 def test_parallel_host_copy(tmp_path):
     """The pooled host copy used by the staged host<->device transfers copies every byte."""
     import shutil
