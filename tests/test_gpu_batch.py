@@ -4,7 +4,7 @@ change results, and admission refuses what does not fit."""
 import numpy as np
 import pytest
 
-from conftest import bits_equal, max_rel
+from conftest import bits_equal, max_rel, wheels_grid
 
 pytestmark = pytest.mark.gpu
 
@@ -24,6 +24,9 @@ def mix(pkg):
         (mg.voronoi_bump_channel(3000, seed=5, thickness=0.06),
          dict(base, eqn="NS", mu=0.01, limiter="NONE", time_step_type="GLOBAL", CFL=0.5, BC1="NO_SLIP_WALL",
               BC2="EXTRAPOLATION", u=mg.mach_speed(0.4))),
+        (wheels_grid(pkg),   # 20-faced cells
+         dict(base, eqn="EULER", limiter="SQUEEZE", time_step_type="GLOBAL", CFL=0.8, BC1="SLIP_WALL",
+              BC2="FREESTREAM", u=mg.mach_speed(0.4), v=5.0)),
     ]
 
 

@@ -9,7 +9,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, bits_equal, max_rel
+from conftest import GOLDEN, bits_equal, max_rel, wheels_grid
 
 pytestmark = pytest.mark.gpu
 
@@ -78,6 +78,32 @@ def test_fp64_polygonal_cells_vs_oracle(opts, pkg, orc):
         assert bits_equal(gpu.get(2), port.get(orc.RES)), f"stage {s}: residual"
         assert bits_equal(gpu.get(0), port.get(orc.QBAR)), f"stage {s}: Qbar"
         # the gradient kernel's own output (limited LSQ gradient of this stage's input) and dt
+        if s % 3 == 0:
+            assert bits_equal(gpu.get(4), port.get(orc.QBAR_GRAD)), f"stage {s}: Qbar gradient"
+        else:
+            assert bits_equal(gpu.get(5), port.get(orc.QSTAR_GRAD)), f"stage {s}: Q* gradient"
+        assert bits_equal(gpu.get(3), port.get(orc.DT)), f"stage {s}: dt"
+    gpu.close()
+
+
+@pytest.mark.parametrize("opts", [
+    dict(eqn="EULER", limiter="SQUEEZE", time_step_type="GLOBAL", CFL=0.8, BC1="SLIP_WALL", BC2="FREESTREAM"),
+    dict(eqn="NS", mu=0.02, limiter="SQUEEZE", time_step_type="LOCAL", CFL=0.5, BC1="NO_SLIP_WALL", BC2="FREESTREAM"),
+], ids=["euler_sq_global", "ns_sq_local"])
+def test_fp64_cells_beyond_16_faces_vs_oracle(opts, pkg, orc):
+    """20-faced cells: the limiter's multi-chunk flag masks, and warps mixing them with 4-faced cells
+    (the warp-shared limiter quotients are taken by whole warps only)."""
+    g = wheels_grid(pkg)
+    assert max(g.sides_histogram()) == 20
+    case = dict(pkg.meshgen.DEFAULT_CASE, u=pkg.meshgen.mach_speed(0.4), v=5.0, **opts)
+    gpu = pkg.Solver(g, case, precision=pkg.FP64)
+    gpu.set_store_residual(True)
+    port = orc.Oracle("port", grid=g, case=case)
+    for s in range(12):
+        gpu.stage()
+        port.stage()
+        assert bits_equal(gpu.get(2), port.get(orc.RES)), f"stage {s}: residual"
+        assert bits_equal(gpu.get(0), port.get(orc.QBAR)), f"stage {s}: Qbar"
         if s % 3 == 0:
             assert bits_equal(gpu.get(4), port.get(orc.QBAR_GRAD)), f"stage {s}: Qbar gradient"
         else:
