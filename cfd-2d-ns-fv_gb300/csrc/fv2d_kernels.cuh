@@ -698,6 +698,22 @@ __device__ __forceinline__ T spectral_sum(const int* __restrict__ inc, const T* 
     return s;
 }
 
+// -x when s == 1, x when s == 0: a sign-bit flip on the integer pipe.  r - t == r + (-t) exactly in
+// IEEE arithmetic (zeros included), so the residual gather adds the flipped contribution instead
+// of branching between += and -= on the incidence's side (a warp's lanes disagree on it).
+__device__ __forceinline__ double neg_if(double x, int s) {
+    return __longlong_as_double(__double_as_longlong(x) ^ ((long long)s << 63));
+}
+__device__ __forceinline__ float neg_if(float x, int s) { return __int_as_float(__float_as_int(x) ^ (s << 31)); }
+
+// x > 0 (false for NaN).  FP64 on the integer pipe: 0 < bits <= bits(+inf).
+template <class T>
+__device__ __forceinline__ bool positive(T x) { return x > T(0); }
+template <>
+__device__ __forceinline__ bool positive<double>(double x) {
+    return (unsigned long long)__double_as_longlong(x) - 1ull < 0x7ff0000000000000ull;
+}
+
 template <class T, int STAGE>
 __device__ __forceinline__ T update_cell(int c, const DevMesh<T>& m, const Q4<T>* __restrict__ tface,
                                          const T* __restrict__ sface, Q4<T>* __restrict__ Qn, Q4<T>* __restrict__ Q1,
@@ -724,13 +740,8 @@ __device__ __forceinline__ T update_cell(int c, const DevMesh<T>& m, const Q4<T>
 #pragma unroll
         for (int u = 0; u < U; u++) {
             if (i0 + u < e) {
-                if (iv[u] & 1) {
 #pragma unroll
-                    for (int j = 0; j < 4; j++) r[j] -= tv[u].p[j];
-                } else {
-#pragma unroll
-                    for (int j = 0; j < 4; j++) r[j] += tv[u].p[j];
-                }
+                for (int j = 0; j < 4; j++) r[j] += neg_if(tv[u].p[j], iv[u] & 1);   // side 1: r -= t
             }
         }
     }
@@ -778,7 +789,7 @@ __device__ __forceinline__ T update_cell(int c, const DevMesh<T>& m, const Q4<T>
                 snext = spectral_sum(inc, sface, b, e);
                 S[c] = snext;
             }
-            if (!(out.p[0] > T(0)) || !(out.p[3] > T(0))) atomicOr(flag, 1);
+            if (!positive(out.p[0]) || !positive(out.p[3])) atomicOr(flag, 1);
             return snext;
         }
     }
@@ -800,7 +811,7 @@ __device__ __forceinline__ T update_cell(int c, const DevMesh<T>& m, const Q4<T>
         snext = spectral_sum(inc, sface, b, e);
         S[c] = snext;
     }
-    if (!(out.p[0] > T(0)) || !(out.p[3] > T(0))) atomicOr(flag, 1);
+    if (!positive(out.p[0]) || !positive(out.p[3])) atomicOr(flag, 1);
     return snext;
 }
 
