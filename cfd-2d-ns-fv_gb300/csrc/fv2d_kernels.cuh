@@ -279,7 +279,7 @@ __device__ __forceinline__ void gradient_cell(int c, const DevMesh<T>& m, const 
         const Q4<T>* __restrict__ fval = sizeof(T) == 8 ? m.fval : nullptr;   // FP64 engine only
         if (!first_stage && !fval) { qp = ldq(Qprev, c); gpx = ldq(Gprev, 2 * c); gpy = ldq(Gprev, 2 * c + 1); }
         if constexpr (sizeof(T) == 8) {
-            // FP64: only about 5 % of the (incidence, component) checks bound the face value and
+            // FP64: only a minority of the (incidence, component) checks bound the face value and
             // need a quotient, but a conditional IEEE division is if-converted (computed for every
             // check).  So one pass flags the checks that need one (bit 4*(incidence - i0) + component,
             // 16 incidences per word) and a second loop takes one flagged check per trip - one
