@@ -178,7 +178,7 @@ __device__ __forceinline__ T pick4(const T a[4], int j) {
 }
 
 #ifndef FV2D_FP64_BLOCK
-#define FV2D_FP64_BLOCK 256   // threads per block of the FP64 gradient and face kernels
+#define FV2D_FP64_BLOCK 128   // threads per block of the FP64 gradient and face kernels
 #endif
 
 // Shared-memory staging of the warp-shared limiter quotients (FP64 single solve, see gradient_cell)
@@ -425,10 +425,11 @@ __device__ __forceinline__ void gradient_cell(int c, const DevMesh<T>& m, const 
 // resident warps.  The FP64 kernels are FP64-pipe-bound; their block size and minimum resident
 // blocks (register cap) set how many warps cover the pipe's latency.
 #ifndef FV2D_FP64_GMINB
-#define FV2D_FP64_GMINB 4   // 64 registers (spilling) and 4 x 46 KB of shared memory: 4 % faster than 2 at 128
+#define FV2D_FP64_GMINB 8   // 8 x 128 threads at 64 registers (spilling), 8 x 23 KB of shared memory:
+                            // 4 % faster than half the warps at 128 registers
 #endif
 #ifndef FV2D_FP64_FMINB
-#define FV2D_FP64_FMINB 1
+#define FV2D_FP64_FMINB 4   // 4 x 128 threads at 116 registers
 #endif
 template <class T>
 constexpr int kStageBlock = sizeof(T) == 4 ? 256 : FV2D_FP64_BLOCK;   // gradient and face kernels
