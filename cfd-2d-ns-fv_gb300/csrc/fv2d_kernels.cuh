@@ -177,6 +177,9 @@ __device__ __forceinline__ T pick4(const T a[4], int j) {
     return j == 0 ? a[0] : j == 1 ? a[1] : j == 2 ? a[2] : a[3];
 }
 
+#ifndef FV2D_FP32_BLOCK
+#define FV2D_FP32_BLOCK 128   // threads per block of the FP32 single-solve gradient and face kernels
+#endif
 #ifndef FV2D_FP64_BLOCK
 #define FV2D_FP64_BLOCK 128   // threads per block of the FP64 gradient and face kernels
 #endif
@@ -432,10 +435,10 @@ __device__ __forceinline__ void gradient_cell(int c, const DevMesh<T>& m, const 
 #define FV2D_FP64_FMINB 4   // 4 x 128 threads at 116 registers
 #endif
 template <class T>
-constexpr int kStageBlock = sizeof(T) == 4 ? 256 : FV2D_FP64_BLOCK;   // gradient and face kernels
+constexpr int kStageBlock = sizeof(T) == 4 ? FV2D_FP32_BLOCK : FV2D_FP64_BLOCK;   // gradient and face kernels
 
 #ifndef FV2D_KG_MINB32
-#define FV2D_KG_MINB32 4   // 61 registers, no spills: 3.5 % faster than 5 blocks at 48 registers
+#define FV2D_KG_MINB32 8   // 8 x 128 threads at 61 registers, no spills: 3.5 % faster than 10 at 48
 #endif
 template <class T, bool SQUEEZE>
 __global__ void __launch_bounds__(kStageBlock<T>, sizeof(T) == 4 ? FV2D_KG_MINB32 : FV2D_FP64_GMINB)
@@ -603,7 +606,7 @@ __device__ __forceinline__ void face_flux(int f, const DevMesh<T>& m, const Q4<T
 }
 
 #ifndef FV2D_KF_MINB32
-#define FV2D_KF_MINB32 5   // 48 registers (16 B spill): 11 % faster than 4 blocks at 63 registers
+#define FV2D_KF_MINB32 10   // 10 x 128 threads at 48 registers (16 B spill): 11 % faster than 8 at 63
 #endif
 template <class T, bool ORDER2, bool NS, bool LAST>
 __global__ void __launch_bounds__(kStageBlock<T>, sizeof(T) == 4 ? FV2D_KF_MINB32 : FV2D_FP64_FMINB)
