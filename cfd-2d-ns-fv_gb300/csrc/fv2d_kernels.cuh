@@ -819,8 +819,11 @@ __device__ __forceinline__ T update_cell(int c, const DevMesh<T>& m, const Q4<T>
     return snext;
 }
 
+#ifndef FV2D_UPD_BLOCK
+#define FV2D_UPD_BLOCK 256   // threads per block of the single-solve update kernel
+#endif
 template <class T, int STAGE>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(FV2D_UPD_BLOCK)
 k_update(int nc, DevMesh<T> m, const Q4<T>* __restrict__ tface, const T* __restrict__ sface, Q4<T>* __restrict__ Qn,
          Q4<T>* __restrict__ Q1, Q4<T>* __restrict__ Q2, T* __restrict__ dt, T* __restrict__ S, T* __restrict__ smax,
          Q4<T>* __restrict__ Rout, int* __restrict__ flag, Consts<T> k, int global_dt, Q4<T>* __restrict__ D,

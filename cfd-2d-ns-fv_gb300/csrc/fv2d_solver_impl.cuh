@@ -215,12 +215,12 @@ public:
         Q4<T>* rout = (store_every_ || s == 2) ? R_ : nullptr;
         launch(K_UPDATE, nc_, [&](int gr) {
             if (s == 0)
-                k_update<T, 0><<<gr, 256, 0, stream_>>>(nc_, dm_, t_, s_, Q_[0], Q_[1], Q_[2], dt_, S_, smax_, rout, flag_, k_, global_dt_, D_, Qlo_);
+                k_update<T, 0><<<gr, FV2D_UPD_BLOCK, 0, stream_>>>(nc_, dm_, t_, s_, Q_[0], Q_[1], Q_[2], dt_, S_, smax_, rout, flag_, k_, global_dt_, D_, Qlo_);
             else if (s == 1)
-                k_update<T, 1><<<gr, 256, 0, stream_>>>(nc_, dm_, t_, s_, Q_[0], Q_[1], Q_[2], dt_, S_, smax_, rout, flag_, k_, global_dt_, D_, Qlo_);
+                k_update<T, 1><<<gr, FV2D_UPD_BLOCK, 0, stream_>>>(nc_, dm_, t_, s_, Q_[0], Q_[1], Q_[2], dt_, S_, smax_, rout, flag_, k_, global_dt_, D_, Qlo_);
             else
-                k_update<T, 2><<<gr, 256, 0, stream_>>>(nc_, dm_, t_, s_, Q_[0], Q_[1], Q_[2], dt_, S_, smax_, rout, flag_, k_, global_dt_, D_, Qlo_);
-        });
+                k_update<T, 2><<<gr, FV2D_UPD_BLOCK, 0, stream_>>>(nc_, dm_, t_, s_, Q_[0], Q_[1], Q_[2], dt_, S_, smax_, rout, flag_, k_, global_dt_, D_, Qlo_);
+        }, FV2D_UPD_BLOCK);
         FV2D_CUDA(cudaGetLastError());
         if (s == 0) { fresh_ = false; init_prims_ = false; }
         last_stage_ = s;
