@@ -271,7 +271,7 @@ def run_reference_arm(args):
 
     def worker(i):
         o = orc.Oracle("port", grid=grid, case=case)
-        o.iterate(1)                       # warm-up (allocation, first touch)
+        o.iterate(args.warmup)             # warm-up iterations (allocation, first touch), untimed
         t = o.time_iterations(iters)
         q.put(t)
 
@@ -293,7 +293,7 @@ def run_reference_arm(args):
                        "parallelism": f"{cores} independent CPU replicas"},
             "cpu_baseline": {"value": value, "unit": "cell-stage/s", "cores": cores, "kind": "port",
                              "sample": f"{iters} SSP-RK3 iterations of the {N}-cell solve per core "
-                                       f"(of {args.steps} steps, capped to ~{REF_SAMPLE_S:.0f} s), after 1 warm-up",
+                                       f"(of {args.steps} steps, capped to ~{REF_SAMPLE_S:.0f} s), after {args.warmup} warm-up iterations",
                              "single_core_value": statistics.median(per_core)},
             "e2e": {"value": value, "unit": "cell-stage/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "wall_s": round(wall, 1)}
