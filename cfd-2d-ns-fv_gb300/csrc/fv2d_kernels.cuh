@@ -297,8 +297,10 @@ __device__ __forceinline__ void gradient_cell(int c, const DevMesh<T>& m, const 
             if constexpr (WARPQ) {
                 constexpr unsigned FULL = 0xffffffffu;
                 // taken by the whole warp or by none of it (the shuffles below need all 32 lanes):
-                // a converged full warp whose cells all have at most 16 faces
-                if (fval != nullptr && __activemask() == FULL && __all_sync(FULL, e - b <= 16)) {
+                // a converged full warp whose cells all have at most 16 faces, in a block no larger
+                // than the one the shared staging is sized for
+                if (fval != nullptr && blockDim.x <= FV2D_FP64_BLOCK && __activemask() == FULL &&
+                    __all_sync(FULL, e - b <= 16)) {
                     unsigned long long mask = 0;
                     for (int i = b; i < e; i++) {
                         Q4<T> qf;
