@@ -62,9 +62,9 @@ __device__ __forceinline__ Q4<T> ldq(const Q4<T>* __restrict__ a, int i) {
 
 // Ordered comparison a < b.  For doubles it runs on the integer pipe: a non-NaN double's bit
 // pattern, with -0 folded onto +0 and the magnitude bits of negatives inverted, orders exactly as
-// IEEE '<' (equal values, +0 and -0 included, give equal keys), and on GB300 the FP64 pipe, which
-// would otherwise execute DSETP, is 1/32 the width of the integer pipe.  (NaN inputs, which only
-// arise in states already flagged as non-physical, may order differently.)
+// IEEE '<' (equal values, +0 and -0 included, give equal keys), and the compare and select issue on
+// the integer ALU pipe instead of taking a DSETP slot on GB300's narrow FP64 pipe.  (NaN inputs,
+// which only arise in states already flagged as non-physical, may order differently.)
 __device__ __forceinline__ long long order_key(double x) {
     long long b = __double_as_longlong(x);
     b = (b == (long long)0x8000000000000000ULL) ? 0LL : b;
