@@ -453,7 +453,8 @@ namespace fv2d {
 void batch_footprint(int precision, long long cells, long long faces, long long incs, long long* bytes) {
     const long long s = precision == FV2D_FP64 ? 8 : 4;
     const long long cell = (precision == FV2D_FP64 ? 9 : 11) * 4 * s + 4 * s + 24 + 4;   // Q[3], G[3], (D, lo), dt, S, vol, 1/vol, LSQ, offsets
-    const long long face = 3 * 4 + 15 * s + 4 * s + s;        // ids, geometry (+ 1/|dist|), contribution, spectral term
+    const long long face = 3 * 4 + 15 * s + 4 * s + s         // ids, geometry (+ 1/|dist|), contribution, spectral term
+                           + (precision == FV2D_FP64 ? 8 * s : 0);   // FP64: stored face states (both sides)
     *bytes = (cells + 1) * cell + faces * face + incs * (8 + 4 * s);
 }
 }  // namespace fv2d

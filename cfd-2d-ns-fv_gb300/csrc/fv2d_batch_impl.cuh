@@ -66,6 +66,9 @@ __device__ __forceinline__ T block_max_t(T v, T* red) {
 // Largest block the batch kernels accept (the autotuner's largest) and the FP32 kernels' minimum
 // resident blocks at that size (their register caps: gradient 64, face 48 - measured fastest);
 // FP64 keeps a 128-register cap.
+#ifndef FV2D_BATCH_FVAL
+#define FV2D_BATCH_FVAL 1   // FP64 batches store the face states for the limiter (0: recompute them)
+#endif
 #ifndef FV2D_KB_MAXT
 #define FV2D_KB_MAXT 256
 #endif
@@ -88,7 +91,8 @@ kb_gradient(const Tile* __restrict__ tiles, const int* __restrict__ ntiles, DevM
         if (sp.order2) {
             if (sp.squeeze) {
                 for (int e = threadIdx.x; e < st.count; e += blockDim.x)
-                    gradient_cell<T, true>(st.start + e, m, Qin, Qprev, Gprev, Gout, sp.k, sp.fresh, sp.init_prims);
+                    gradient_cell<T, true, sizeof(T) == 8, FV2D_KB_MAXT / 32>(st.start + e, m, Qin, Qprev, Gprev, Gout, sp.k,
+                                                                             sp.fresh, sp.init_prims);
             } else {
                 for (int e = threadIdx.x; e < st.count; e += blockDim.x)
                     gradient_cell<T, false>(st.start + e, m, Qin, Qprev, Gprev, Gout, sp.k, sp.fresh, sp.init_prims);
@@ -293,6 +297,10 @@ public:
         size_t oflag = take(4 * (size_t)S_);
         const bool comp = sizeof(T) == 4;   // FP32: delta-form increments + compensated base state
         size_t oD = comp ? take(q4 * Nc_) : 0, olo = comp ? take(q4 * Nc_) : 0;
+        // FP64: the face pass stores its reconstructed face states for the next squeeze (as the
+        // single-solve FP64 engine does); a solve's first stage after admission uses the sentinel
+        const bool fv = !comp && FV2D_BATCH_FVAL;
+        size_t ofval = fv ? take(2 * q4 * Fc_) : 0;
         tile_cap_ = (int)std::min<long long>((Nc_ + Fc_) / 64 + 4 * (long long)S_ + 16, 1LL << 28);
         size_t otc = take(sizeof(Tile) * tile_cap_), otf = take(sizeof(Tile) * tile_cap_), ocnt = take(64);
         bytes_ = off;
@@ -317,6 +325,7 @@ public:
         m_.g.my = geo_[10]; m_.g.lx = geo_[11]; m_.g.ly = geo_[12]; m_.g.dist = geo_[13];
         m_.Ixx = ixx; m_.Iyy = iyy; m_.Ixy = ixy; m_.vol = vol;
         m_.rvol = (T*)(a + orvol); m_.rdist = (T*)(a + ordist);
+        m_.fval = fv ? (Q4<T>*)(a + ofval) : nullptr;
         FV2D_B(cudaMemsetAsync(arena_, 0, bytes_, stream_));
         FV2D_B(cudaStreamSynchronize(stream_));
         cells_.reset(Nc_);

@@ -196,7 +196,7 @@ struct WarpQ {
     double quo[WARPS][FV2D_WARPQ_CAP];                              // the checks' quotients
 };
 
-template <class T, bool SQUEEZE, bool WARPQ = false>
+template <class T, bool SQUEEZE, bool WARPQ = false, int QWARPS = FV2D_FP64_BLOCK / 32>
 __device__ __forceinline__ void gradient_cell(int c, const DevMesh<T>& m, const Q4<T>* __restrict__ Q,
                                               const Q4<T>* __restrict__ Qprev, const Q4<T>* __restrict__ Gprev,
                                               Q4<T>* __restrict__ Gout, const Consts<T>& k, int first_stage,
@@ -298,8 +298,8 @@ __device__ __forceinline__ void gradient_cell(int c, const DevMesh<T>& m, const 
                 constexpr unsigned FULL = 0xffffffffu;
                 // taken by the whole warp or by none of it (the shuffles below need all 32 lanes):
                 // a converged full warp whose cells all have at most 16 faces, in a block no larger
-                // than the one the shared staging is sized for
-                if (fval != nullptr && blockDim.x <= FV2D_FP64_BLOCK && __activemask() == FULL &&
+                // than the one the shared staging is sized for (QWARPS warps)
+                if (fval != nullptr && blockDim.x <= 32 * QWARPS && __activemask() == FULL &&
                     __all_sync(FULL, e - b <= 16)) {
                     unsigned long long mask = 0;
                     for (int i = b; i < e; i++) {
@@ -324,7 +324,7 @@ __device__ __forceinline__ void gradient_cell(int c, const DevMesh<T>& m, const 
                     }
                     const int total = __shfl_sync(FULL, incl, 31), excl = incl - cnt;
                     if (total <= FV2D_WARPQ_CAP) {
-                        __shared__ WarpQ<FV2D_FP64_BLOCK / 32> sq;
+                        __shared__ WarpQ<QWARPS> sq;
 #pragma unroll
                         for (int j = 0; j < 4; j++) {
                             sq.qc[w][j][lane] = qc.p[j];
