@@ -77,8 +77,11 @@ __device__ __forceinline__ T block_max_t(T v, T* red) {
 #endif
 constexpr int kBatchMaxBlock = FV2D_KB_MAXT;
 constexpr int kBatchMinB64 = 512 / FV2D_KB_MAXT;
+#ifndef FV2D_KBG_MINB64
+#define FV2D_KBG_MINB64 kBatchMinB64
+#endif
 template <class T>
-__global__ void __launch_bounds__(FV2D_KB_MAXT, sizeof(T) == 4 ? FV2D_KBG_MINB32 : kBatchMinB64)
+__global__ void __launch_bounds__(FV2D_KB_MAXT, sizeof(T) == 4 ? FV2D_KBG_MINB32 : FV2D_KBG_MINB64)
 kb_gradient(const Tile* __restrict__ tiles, const int* __restrict__ ntiles, DevMesh<T> m,
             const SolveParams<T>* __restrict__ P, const Q4<T>* __restrict__ Qin, const Q4<T>* __restrict__ Qprev,
             const Q4<T>* __restrict__ Gprev, Q4<T>* __restrict__ Gout) {
