@@ -63,12 +63,13 @@ __device__ __forceinline__ T block_max_t(T v, T* red) {
     return s;   // valid in thread 0
 }
 
-// Largest block the batch kernels accept (the autotuner's largest) and the FP32 kernels' minimum
-// resident blocks at that size (their register caps: gradient 64, face 48 - measured fastest);
-// FP64 keeps a 128-register cap.
 #ifndef FV2D_BATCH_FVAL
 #define FV2D_BATCH_FVAL 1   // FP64 batches store the face states for the limiter (0: recompute them)
 #endif
+
+// Largest block the batch kernels accept (the autotuner's largest) and the FP32 kernels' minimum
+// resident blocks at that size (their register caps: gradient 64, face 48 - measured fastest);
+// FP64 keeps a 128-register cap.
 #ifndef FV2D_KB_MAXT
 #define FV2D_KB_MAXT 256
 #endif
