@@ -512,7 +512,15 @@ def run_gpu_arm(args):
     roof["peak_source"] = f"{peak_kind} hbm_gbs"
     roof["traffic"] = ncu_traffic(args.precision, dom, N, F)
     if prec == pkg.FP64:   # this path is bound by the FP64 pipe, not HBM
-        roof["fp64_pipe"] = fp64_pipe(per, N, F, clk.get("sm_mhz") or clk.get("sm_max_mhz") or 2070.0)
+        fp = fp64_pipe(per, N, F, clk.get("sm_mhz") or clk.get("sm_max_mhz") or 2070.0)
+        if fp:
+            # the whole step: every stage kernel's FP64 pipe slots per iteration (three launches of
+            # each) over the graph-replayed iteration time
+            it_inst = 3 * sum(v["inst_per_launch"] for v in fp["per_kernel"].values())
+            it_ach = it_inst / (ms / args.steps * 1e-3) / 1e9
+            fp["iteration"] = {"inst": it_inst, "ms": round(ms / args.steps, 4), "achieved": round(it_ach, 1),
+                               "frac": round(it_ach / fp["peak"], 3)}
+        roof["fp64_pipe"] = fp
     gpu_launches = 3 * 3 * args.steps
 
     # ---- end to end through the C ABI with host buffers: upload Qbar, one iteration, download
