@@ -8,14 +8,15 @@ CFL 0.5: the reference scheme itself (checked with the bit-exact oracle) diverge
 wall within 5-25 iterations for any CFL from 0.6 to 0.9 on this mesh; the work per iteration does
 not depend on the CFL number.
 One step = one SSP-RK3 iteration = 3 x num_cells cell-stage updates.  The solve's device arrays
-(~1.2 GB) are larger than the 129 MB L2, so no flush is needed between steps.
+(~1.4 GB) are larger than the 129 MB L2, so no flush is needed between steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--cells C]
                   [--only fp32|batched|serve|precision] [--no-fp32] [--no-batch] [--no-serve] [--no-cpu]
 
 The JSON line: `value` (device-timed graph replay), `e2e` (the C ABI with page-locked host buffers,
 H2D + step + D2H + residual norm each step; `pageable_value` with ordinary arrays), `roofline`
-(dominant kernel against the measured HBM peak, plus `fp64_pipe` against the FP64 issue peak),
+(dominant kernel against the measured HBM peak, plus `fp64_pipe` against the FP64 issue peak: per
+kernel, and for the whole graph-replayed iteration in `fp64_pipe.iteration`),
 `cpu_baseline` (the oracle port on one host core), and the FP32, c4 batch and c5 serving lines.
 --impl reference times the reference's CPU solver step (the oracle port, a line-by-line
 restatement proven bit-identical to the reference) on the host cores: one independent replica of
