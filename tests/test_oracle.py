@@ -111,3 +111,23 @@ def test_port_handles_more_than_six_sides(pkg, orc):
     port.stage(6)
     q = port.get(orc.QBAR)
     assert np.all(np.isfinite(q))
+
+
+def test_port_handles_twenty_faced_cells(pkg, orc):
+    """20-faced hub cells (the limiter's multi-chunk masks on the GPU): the port runs them, and with
+    FREESTREAM on every boundary a uniform freestream stays uniform (the face normals times areas of
+    each closed cell sum to zero), so its residual is round-off next to the residual the same mesh
+    has with slip walls."""
+    from conftest import wheels_grid
+    g = wheels_grid(pkg)
+    assert max(g.sides_histogram()) == 20
+    base = dict(pkg.meshgen.DEFAULT_CASE, eqn="EULER", u=pkg.meshgen.mach_speed(0.4), v=5.0, limiter="SQUEEZE",
+                time_step_type="LOCAL", BC2="FREESTREAM")
+    walls = orc.Oracle("port", grid=g, case=dict(base, BC1="SLIP_WALL"))
+    walls.stage(1)
+    r_walls = np.abs(walls.get(orc.RES)).max()
+    walls.stage(5)
+    assert np.all(np.isfinite(walls.get(orc.QBAR)))
+    free = orc.Oracle("port", grid=g, case=dict(base, BC1="FREESTREAM"))
+    free.stage(1)
+    assert np.abs(free.get(orc.RES)).max() < 1e-12 * r_walls
