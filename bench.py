@@ -32,6 +32,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -76,14 +77,14 @@ class Clocks:
     def __init__(self, gpu_index):
         self.gpu = gpu_index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+        self.path = os.path.join(tempfile.gettempdir(), f"fv2d_bench_clocks_{os.getpid()}.csv")
 
     def start(self):
         try:
             os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                                          "-lms", "100"], stdout=self.fh, stderr=subprocess.DEVNULL)
+                                          "-lms", "25"], stdout=self.fh, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
 
@@ -97,8 +98,13 @@ class Clocks:
             self.proc.kill()
         self.fh.close()
         sm, smax, reasons = [], [], set()
+        lines = open(self.path).read().splitlines()
+        try:
+            os.remove(self.path)
+        except OSError:
+            pass
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in open(self.path):
+        for line in lines:
             f = [x.strip() for x in line.split(",")]
             if len(f) < 9:
                 continue
@@ -157,6 +163,42 @@ def bytes_per_launch(kernel, N, F, ninc, Nb, s, ns, squeeze, comp=False, store_r
             b += (N * 4 * s) / 3.0               # residual stored on the last stage
         return b
     return 0.0
+
+
+def bytes_8d(N, F, Nb, s, ns=False, squeeze=True, euler_geometry=False):
+    """Algorithmic bytes of one RK stage of one solve by the benchmark specification's formula (a
+    two-pass design, every array counted once per stage):
+        B = N (40.67 s + 28) + F (g s + 8) + 4 (2F - Nb)
+    per cell: stage state read 4s, Qn read on stages 2-3 (8/3)s, state written 4s, gradient written
+    and read 16s, previous stage's state and limited gradient for the squeeze limiter 12s, dt s,
+    volume s, LSQ moments 24 B (always FP64), CSR offset 4 B; per face: g = 9 geometry values
+    (nx ny A d1x d1y d2x d2y dxj dyj) plus 5 for NS (mx my lx ly dist), cell ids 8 B; per incidence:
+    the face id 4 B.  euler_geometry: count 9 geometry values for NS meshes too.
+    s = state bytes (8 FP64, 4 FP32)."""
+    per_cell = (4 + 8.0 / 3.0 + 4 + 16 + (12 if squeeze else 0) + 1 + 1) * s + 24 + 4
+    g = 9 + (5 if (ns and not euler_geometry) else 0)
+    return N * per_cell + F * (g * s + 8) + 4 * (2 * F - Nb)
+
+
+def step_8d(solves, ms_per_iteration, peak):
+    """Whole-step HBM fraction on the specification's algorithmic bytes: `solves` is a list of
+    (N, F, Nb, s, ns, squeeze); one iteration is 3 stages of each.  Reported with the NS geometry term
+    (the formula as specified) and with Euler geometry for every solve (the smaller byte count)."""
+    out = {}
+    for key, eg in (("", False), ("_euler_geometry", True)):
+        b = 3.0 * sum(bytes_8d(N, F, Nb, s, ns, sq, euler_geometry=eg) for N, F, Nb, s, ns, sq in solves)
+        ach = b / (ms_per_iteration * 1e-3) / 1e9
+        cells = sum(x[0] for x in solves)
+        out["bytes_per_cell_stage" + key] = round(b / (3.0 * cells), 1)
+        out["achieved" + key] = round(ach, 1)
+        out["frac" + key] = round(ach / peak, 4)
+    return out
+
+
+def add_step_8d(roof, solves, ms_per_iteration, peak):
+    """Put the whole-step fraction on the specification's bytes into a roofline dict as scalars."""
+    for k, v in step_8d(solves, ms_per_iteration, peak).items():
+        roof["step_8d_" + k] = v
 
 
 def roofline(kt, kbytes, peak):
@@ -223,12 +265,15 @@ def peaks():
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def cpu_baseline(pkg, orc, grid, case, iters):
+def cpu_baseline(pkg, orc, grid, case, iters, samples):
+    """The oracle port on one host core: `samples` timed samples of `iters` iterations each after one
+    warm-up iteration; the median sample's rate (the shared host's rate drifts from run to run)."""
     o = orc.Oracle("port", grid=grid, case=case)
     o.iterate(1)                                   # first iteration includes allocation warm-up
-    t = o.time_iterations(iters)
+    ts = [o.time_iterations(iters) for _ in range(samples)]
     N = grid.num_cells
-    return 3.0 * N * iters / t, t
+    rates = [3.0 * N * iters / t for t in ts]
+    return statistics.median(rates), sum(ts), [round(r, 1) for r in rates]
 
 
 def max_over_ranks(x: float, ws: int) -> float:
@@ -328,6 +373,7 @@ def measure_fp32(pkg, grid, case, args, peak, peak_kind, N, F, ninc, Nb):
     dom, roof, per = roofline(kt, single_kernel_bytes(N, F, ninc, Nb, 4, True), peak)
     roof["peak_source"] = f"{peak_kind} hbm_gbs"
     roof["traffic"] = ncu_traffic("fp32", dom, N, F)
+    add_step_8d(roof, [(N, F, Nb, 4, case["eqn"] == "NS", case["limiter"] == "SQUEEZE")], ms / args.steps, peak)
     return {"value": 3.0 * N * args.steps / (ms * 1e-3), "unit": "cell-stage/s", "ms_per_step": ms / args.steps,
             "roofline": roof,
             "kernels": {k: {"avg_ms": round(v["avg_ms"], 4), "gbs": round(v["bytes"] / (v["avg_ms"] * 1e-3) / 1e9, 1)}
@@ -376,6 +422,8 @@ def measure_batched(pkg, args, peak, peak_kind):
     dom, roof, per = roofline(kt, kbytes, peak)
     roof["peak_source"] = f"{peak_kind} hbm_gbs"
     roof["traffic"] = ncu_traffic("batch_fp32", dom, tot_c, tot_f)
+    add_step_8d(roof, [(g.num_cells, g.num_faces, int((g.fc2 <= 0).sum()), 4, bool(sp["ns"]), True)
+                       for g, sp in zip(grids, specs)], ms / args.steps, peak)
     norms = b.norms()
     finite = all(np.all(np.isfinite(v[0])) for v in norms.values())
     b.close()
@@ -401,8 +449,16 @@ def measure_serving(pkg, args):
     cells, faces, solves = serve.capacity_from_budget(pool, budget)
     b = pkg.Batch(cells, faces, solves, precision=pkg.FP32)
     b.set_grid_mode(True)
+    peak, _ = peaks()
+
+    def stage_bytes(g, spec):
+        return bytes_8d(g.num_cells, g.num_faces, int((g.fc2 <= 0).sum()), 4, bool(spec["ns"]), True)
+
     out = serve.serve(b, stream, pool, duration=args.serve_seconds, target=1e-6, max_iters=args.serve_max_iters,
-                      check_every=25, stall_iters=args.serve_stall_iters)
+                      check_every=25, stall_iters=args.serve_stall_iters, stage_bytes=stage_bytes)
+    if out.get("bytes_per_s"):
+        out["step_8d_achieved"] = round(out["bytes_per_s"] / 1e9, 1)
+        out["step_8d_frac"] = round(out["bytes_per_s"] / 1e9 / peak, 4)
     usage = b.usage()
     b.close()
     base = serve.serve_one_at_a_time(stream, pool, duration=args.serve_seconds, precision=pkg.FP64, target=1e-6,
@@ -521,7 +577,12 @@ def run_gpu_arm(args):
             it_ach = it_inst / (ms / args.steps * 1e-3) / 1e9
             fp["iteration"] = {"inst": it_inst, "ms": round(ms / args.steps, 4), "achieved": round(it_ach, 1),
                                "frac": round(it_ach / fp["peak"], 3)}
+            roof["fp64_pipe_iteration_frac"] = fp["iteration"]["frac"]
         roof["fp64_pipe"] = fp
+        if fp:
+            roof["fp64_pipe_frac"] = fp["frac"]
+            roof["fp64_pipe_kernel"] = fp["kernel"]
+    add_step_8d(roof, [(N, F, Nb, s_bytes, True, True)], ms / args.steps, peak)
     gpu_launches = 3 * 3 * args.steps
 
     # ---- end to end through the C ABI with host buffers: upload Qbar, one iteration, download
@@ -570,9 +631,11 @@ def run_gpu_arm(args):
     if rank == 0 and not args.no_cpu:
         orc = entry.load_oracle()
         orc.build(ref_dir="/nonexistent")
-        cv, ct = cpu_baseline(pkg, orc, grid, case, args.cpu_iters)
+        cv, ct, rates = cpu_baseline(pkg, orc, grid, case, args.cpu_iters, args.cpu_samples)
         cpu = {"value": cv, "unit": "cell-stage/s", "cores": 1, "kind": "port",
-               "sample": f"{args.cpu_iters} SSP-RK3 iterations of the same {N}-cell solve ({ct:.1f} s), after 1 warm-up"}
+               "sample": f"median of {args.cpu_samples} samples of {args.cpu_iters} SSP-RK3 iterations of the same "
+                         f"{N}-cell solve ({ct:.1f} s in all), after 1 warm-up iteration",
+               "samples": rates}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "cell-stage/s", "n_gpus": ws, "steps": args.steps,
@@ -603,7 +666,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cells", type=int, default=1_000_000)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
-    ap.add_argument("--cpu-iters", type=int, default=4)
+    ap.add_argument("--cpu-iters", type=int, default=2)
+    ap.add_argument("--cpu-samples", type=int, default=5)
     ap.add_argument("--cpu-cores", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp32", action="store_true")

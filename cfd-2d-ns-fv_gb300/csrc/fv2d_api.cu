@@ -63,8 +63,8 @@ int check_case(const fv2d_case* cs) {
     if (cs->order != 1 && cs->order != 2)
         return fail(FV2D_ERR_CASE, "solution_poly_order must be 0 or 1 (res.cpp:56-58 rejects other orders)");
     if (cs->eqn != FV2D_EULER && cs->eqn != FV2D_NS) return fail(FV2D_ERR_CASE, "eqn must be EULER or NS");
-    if (cs->flux_solver != FV2D_RUSANOV)
-        return fail(FV2D_ERR_CASE, "flux_solver must be RUSANOV (the reference's ROE path is unfinished: res.cpp:66-68)");
+    if (cs->flux_solver != FV2D_RUSANOV && cs->flux_solver != FV2D_ROE)
+        return fail(FV2D_ERR_CASE, "flux_solver must be RUSANOV or ROE");
     if (cs->limiter != FV2D_LIM_NONE && cs->limiter != FV2D_LIM_MINMOD && cs->limiter != FV2D_LIM_SQUEEZE)
         return fail(FV2D_ERR_CASE, "limiter must be NONE, MINMOD or SQUEEZE");
     if (cs->time_type != FV2D_DT_GLOBAL && cs->time_type != FV2D_DT_LOCAL)

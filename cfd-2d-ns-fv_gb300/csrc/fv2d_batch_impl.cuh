@@ -8,8 +8,10 @@
 // parameters into shared memory once per tile and applies the same per-element code.  One
 // iteration (3 stages x 3 kernels + 2 memsets) is captured in a CUDA graph; since the graph reads
 // the tile lists and parameter table from device memory, solves can join and leave between
-// iterations without re-capturing.  Per-solve reductions (GLOBAL dt maximum, residual L2 sums)
-// use one atomic per tile.
+// iterations without re-capturing.  Per-solve reductions: the GLOBAL dt maximum uses one atomic
+// max per tile (a maximum does not depend on the order); the residual L2 sums are written per tile
+// and summed per solve over its tiles in a fixed order (kb_res_norm), so they are reproducible bit
+// for bit from run to run.
 #pragma once
 
 #include <algorithm>
@@ -138,7 +140,7 @@ template <class T, int STAGE>
 __global__ void __launch_bounds__(FV2D_KB_MAXT)
 kb_update(const Tile* __restrict__ tiles, const int* __restrict__ ntiles, DevMesh<T> m, SolveParams<T>* P,
           const Q4<T>* __restrict__ tface, const T* __restrict__ sface, Q4<T>* __restrict__ Qn, Q4<T>* __restrict__ Q1,
-          Q4<T>* __restrict__ Q2, T* __restrict__ dt, T* __restrict__ S, T* __restrict__ smax, double* __restrict__ res2,
+          Q4<T>* __restrict__ Q2, T* __restrict__ dt, T* __restrict__ S, T* __restrict__ smax, double* __restrict__ tpart,
           int* __restrict__ flags, Q4<T>* __restrict__ D, Q4<T>* __restrict__ Qlo) {
     __shared__ SolveParams<T> sp;
     __shared__ Tile st;
@@ -167,12 +169,40 @@ kb_update(const Tile* __restrict__ tiles, const int* __restrict__ ntiles, DevMes
 #pragma unroll
             for (int j = 0; j < 4; j++) {
                 const double bs = block_sum(acc[j], redd);
-                if (threadIdx.x == 0) atomicAdd(res2 + 4 * st.sid + j, bs);
+                if (threadIdx.x == 0) tpart[4 * (size_t)t + j] = bs;   // this tile's sum of squares
             }
         }
         if (STAGE == 0 && threadIdx.x == 0) { P[st.sid].fresh = 0; P[st.sid].init_prims = 0; }
         __syncthreads();
     }
+}
+
+// Per-solve residual sums of squares: solve s owns the cell tiles [srange[2s], srange[2s] +
+// srange[2s+1]) of the tile list; one block per solve slot adds their per-tile sums (kb_update,
+// last stage) in a fixed order - a strided pass per thread, then the block's fixed-shape tree - so
+// the result is the same bits on every run.  A slot without tiles gets zeros.  (A template only so
+// that each precision's translation unit may include it.)
+template <class T>
+__global__ void __launch_bounds__(256)
+kb_res_norm(const int* __restrict__ srange, const double* __restrict__ tpart, double* __restrict__ res2) {
+    __shared__ double sh[4][256];
+    const int s = blockIdx.x, first = srange[2 * s], n = srange[2 * s + 1];
+    double acc[4] = {0, 0, 0, 0};
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[j] += tpart[4 * (size_t)(first + i) + j];
+#pragma unroll
+    for (int j = 0; j < 4; j++) sh[j][threadIdx.x] = acc[j];
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h)
+#pragma unroll
+            for (int j = 0; j < 4; j++) sh[j][threadIdx.x] += sh[j][threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int j = 0; j < 4; j++) res2[4 * s + j] = sh[j][0];
 }
 
 // A newly admitted solve's ids: solve-local -> arena (CSR offsets + i0, face ids + f0, cell ids + c0;
@@ -307,6 +337,7 @@ public:
         size_t ofval = fv ? take(2 * q4 * Fc_) : 0;
         tile_cap_ = (int)std::min<long long>((Nc_ + Fc_) / 64 + 4 * (long long)S_ + 16, 1LL << 28);
         size_t otc = take(sizeof(Tile) * tile_cap_), otf = take(sizeof(Tile) * tile_cap_), ocnt = take(64);
+        size_t otp = take(32 * (size_t)tile_cap_), osr = take(8 * (size_t)S_);
         bytes_ = off;
         FV2D_B(cudaMalloc(&arena_, bytes_));
         char* a = (char*)arena_;
@@ -320,6 +351,7 @@ public:
         t_ = (Q4<T>*)(a + ot); s_ = (T*)(a + os);
         P_ = (SolveParams<T>*)(a + oP); smax_ = (T*)(a + osmax); res2_ = (double*)(a + ores); flags_ = (int*)(a + oflag);
         tc_ = (Tile*)(a + otc); tf_ = (Tile*)(a + otf); cnt_ = (int*)(a + ocnt);
+        tpart_ = (double*)(a + otp); srange_ = (int*)(a + osr);
         D_ = comp ? (Q4<T>*)(a + oD) : nullptr;
         Qlo_ = comp ? (Q4<T>*)(a + olo) : nullptr;
         m_.inc_off = incoff; m_.inc = inc; m_.nbr = nbr; m_.fc1 = fc1; m_.fc2 = fc2; m_.qcell = qc;
@@ -459,6 +491,7 @@ public:
         p.k.two_cfl = (T)(2 * cs->cfl);
         p.k.vn0 = (T)std::sqrt(cs->v * cs->v + cs->u * cs->u);
         p.k.c0 = (T)std::sqrt(cs->gamma * (cs->P / cs->rho));
+        p.k.roe = cs->flux_solver == FV2D_ROE;
         p.order2 = cs->order == 2; p.ns = cs->eqn == FV2D_NS; p.squeeze = cs->limiter == FV2D_LIM_SQUEEZE;
         p.global_dt = cs->time_type == FV2D_DT_GLOBAL; p.fresh = 1; p.init_prims = 1;
         pin_params_[sid] = p;   // a slot is rewritten only after its solve was removed (synchronised)
@@ -616,17 +649,21 @@ private:
     int rebuild_tiles() {
         tiles_dirty_ = false;
         std::vector<Tile> tc, tf;
+        std::vector<int> sr(2 * (size_t)S_, 0);   // per solve slot: first cell tile, cell tile count
         for (int s = 0; s < S_; s++) {
             const Rec& r = recs_[s];
+            sr[2 * s] = (int)tc.size();
             if (!r.active) continue;
             const long long tile = (long long)tune_.block * tune_.tile_mult[bucket(r.n)];
             for (long long c = 0; c < r.n; c += tile) tc.push_back(Tile{s, (int)(r.c0 + c), (int)std::min(tile, r.n - c), 0});
             for (long long f = 0; f < r.m; f += tile) tf.push_back(Tile{s, (int)(r.f0 + f), (int)std::min(tile, r.m - f), 0});
+            sr[2 * s + 1] = (int)tc.size() - sr[2 * s];
         }
         if ((int)tc.size() > tile_cap_ || (int)tf.size() > tile_cap_) { err_ = "tile list capacity exceeded"; return FV2D_ERR_NOMEM; }
         // asynchronous upload through a page-locked buffer; an event guards the buffer until the
         // previous upload has been read (the graph reads the device lists in stream order)
-        const size_t bt = sizeof(Tile) * tc.size(), bf = sizeof(Tile) * tf.size(), need = bt + bf + 64;
+        const size_t bt = sizeof(Tile) * tc.size(), bf = sizeof(Tile) * tf.size(), bs = 4 * sr.size();
+        const size_t need = bt + bf + bs + 64;
         FV2D_B(cudaEventSynchronize(tiles_free_));
         if (need > tile_pin_bytes_) {
             if (tile_pin_) cudaFreeHost(tile_pin_);
@@ -641,8 +678,10 @@ private:
         char* tp = tile_pin_ + 64;
         if (bt) std::memcpy(tp, tc.data(), bt);
         if (bf) std::memcpy(tp + bt, tf.data(), bf);
+        std::memcpy(tp + bt + bf, sr.data(), bs);
         if (bt) FV2D_B(cudaMemcpyAsync(tc_, tp, bt, cudaMemcpyHostToDevice, stream_));
         if (bf) FV2D_B(cudaMemcpyAsync(tf_, tp + bt, bf, cudaMemcpyHostToDevice, stream_));
+        FV2D_B(cudaMemcpyAsync(srange_, tp + bt + bf, bs, cudaMemcpyHostToDevice, stream_));
         FV2D_B(cudaMemcpyAsync(cnt_, cnt, 2 * sizeof(int), cudaMemcpyHostToDevice, stream_));
         FV2D_B(cudaEventRecord(tiles_free_, stream_));
         n_ctiles_ = (int)tc.size();
@@ -704,18 +743,16 @@ private:
                 else
                     kb_face<T, false><<<gf_[0], B, 0, stream_>>>(tf_, nft, m_, P_, Q_[s], G_[s], t_, s_);
             });
-            if (s == 2) {
-                FV2D_B(cudaMemsetAsync(smax_, 0, sizeof(T) * S_, stream_));
-                FV2D_B(cudaMemsetAsync(res2_, 0, 32 * (size_t)S_, stream_));
-            }
+            if (s == 2) FV2D_B(cudaMemsetAsync(smax_, 0, sizeof(T) * S_, stream_));
             timed(2, [&] {
                 if (s == 0)
-                    kb_update<T, 0><<<gu_[0], B, 0, stream_>>>(tc_, nct, m_, P_, t_, s_, Q_[0], Q_[1], Q_[2], dt_, S_arr_, smax_, res2_, flags_, D_, Qlo_);
+                    kb_update<T, 0><<<gu_[0], B, 0, stream_>>>(tc_, nct, m_, P_, t_, s_, Q_[0], Q_[1], Q_[2], dt_, S_arr_, smax_, tpart_, flags_, D_, Qlo_);
                 else if (s == 1)
-                    kb_update<T, 1><<<gu_[1], B, 0, stream_>>>(tc_, nct, m_, P_, t_, s_, Q_[0], Q_[1], Q_[2], dt_, S_arr_, smax_, res2_, flags_, D_, Qlo_);
+                    kb_update<T, 1><<<gu_[1], B, 0, stream_>>>(tc_, nct, m_, P_, t_, s_, Q_[0], Q_[1], Q_[2], dt_, S_arr_, smax_, tpart_, flags_, D_, Qlo_);
                 else
-                    kb_update<T, 2><<<gu_[2], B, 0, stream_>>>(tc_, nct, m_, P_, t_, s_, Q_[0], Q_[1], Q_[2], dt_, S_arr_, smax_, res2_, flags_, D_, Qlo_);
+                    kb_update<T, 2><<<gu_[2], B, 0, stream_>>>(tc_, nct, m_, P_, t_, s_, Q_[0], Q_[1], Q_[2], dt_, S_arr_, smax_, tpart_, flags_, D_, Qlo_);
             });
+            if (s == 2) kb_res_norm<T><<<S_, 256, 0, stream_>>>(srange_, tpart_, res2_);
             FV2D_B(cudaGetLastError());
         }
         return FV2D_OK;
@@ -744,6 +781,8 @@ private:
     Q4<T>* Qlo_ = nullptr;   // FP32 only: compensation term of Qn
     SolveParams<T>* P_ = nullptr;
     double* res2_ = nullptr;
+    double* tpart_ = nullptr;   // per cell tile: residual sums of squares of the last stage
+    int* srange_ = nullptr;     // per solve slot: first cell tile and tile count
     int* flags_ = nullptr;
     Tile *tc_ = nullptr, *tf_ = nullptr;
     int* cnt_ = nullptr;

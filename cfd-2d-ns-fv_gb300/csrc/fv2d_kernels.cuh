@@ -29,6 +29,10 @@ struct Consts {
     T rho_inf, u_inf, v_inf, P_inf;    // freestream primitives (initial Qbar primitives)
     T two_cfl;                         // 2*CFL
     T vn0, c0;                         // initial Vn_avg, c_avg (class_q.hpp:61-62)
+    // flux_solver = ROE: the reference's res() calls no flux routine (res.cpp:62-69), so the
+    // inviscid flux of every face is class_F::init's -101 (class_f.hpp:26-30) and Vn_avg, c_avg
+    // (the time step's spectral terms) keep their initial values
+    int roe;
 };
 
 // Face geometry, SoA, device order.
@@ -532,7 +536,7 @@ __device__ __forceinline__ void face_flux(int f, const DevMesh<T>& m, const Q4<T
     const T lam = (fabs(vna) + ca) / T(2);
     T Fr[4];
 #pragma unroll
-    for (int j = 0; j < 4; j++) Fr[j] = (F1[j] + F2[j]) / T(2) - lam * (Rq[j] - L[j]);
+    for (int j = 0; j < 4; j++) Fr[j] = k.roe ? T(-101) : (F1[j] + F2[j]) / T(2) - lam * (Rq[j] - L[j]);
 
     // viscous flux (first order never adds it: res.cpp:27-29,50-53)
     T V[4] = {T(0), T(0), T(0), T(0)};
@@ -604,7 +608,7 @@ __device__ __forceinline__ void face_flux(int f, const DevMesh<T>& m, const Q4<T
         else t.p[j] = (V[j] * A) - (Fr[j] * A);
     }
     tout[f] = t;
-    if (LAST) sout[f] = (fabs(vna) + ca) * A;
+    if (LAST) sout[f] = k.roe ? (fabs(k.vn0) + k.c0) * A : (fabs(vna) + ca) * A;
 }
 
 #ifndef FV2D_KF_MINB32

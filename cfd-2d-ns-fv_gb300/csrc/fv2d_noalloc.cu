@@ -6,7 +6,11 @@
 // library would fail or fragment that pool), or a latency-critical thread that must not call
 // cudaMalloc/cudaFree because they can synchronise the whole device.  Such a caller passes its
 // inputs and outputs as device pointers it already owns; the only extra memory is the static array
-// below, which every GPU that loads this library holds until the process exits.
+// below, which lives with this library's device code on each GPU until the process exits.  With
+// CUDA's lazy module loading (the default) that code and the array are placed on a device by the
+// first call there, so that first call takes device memory and later calls take none: callers
+// whose allocator reserves the GPU make one warm-up call per device before reserving, or set
+// CUDA_MODULE_LOADING=EAGER.
 //
 // Built with -fmad=false, like the FP64 engine, so its arithmetic rounds like the rest of the FP64
 // path.  The existing entry points and kernels are untouched.
@@ -33,6 +37,8 @@ double* g_scratch_addr[kMaxDevices] = {nullptr};
 
 // One-time set-up per device, with that device current: the device address of the scratch
 // array.  In host code the symbol's name is only a host-side stand-in, never a device address.
+// The address is cached per device ordinal for the life of the process; it belongs to the
+// device's primary context, so a device reset after the first call is not supported.
 int scratch_address(double** out) {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
@@ -141,6 +147,7 @@ extern "C" int fv2d_residual_noalloc(const fv2d_noalloc_mesh* m, const fv2d_case
         return FV2D_ERR_ARG;
     }
     if (!(cs->gamma > 1) || !(cs->rho > 0) || !(cs->P > 0)) { set_global_error("gamma > 1, rho > 0, P > 0 required"); return FV2D_ERR_CASE; }
+    if (cs->flux_solver != FV2D_RUSANOV) { set_global_error("flux_solver must be RUSANOV"); return FV2D_ERR_CASE; }
     double* scratch = nullptr;
     int rc = scratch_address(&scratch);
     if (rc) return rc;

@@ -57,6 +57,7 @@ public:
         k_.two_cfl = (T)(2 * cs.cfl);
         k_.vn0 = (T)std::sqrt(cs.v * cs.v + cs.u * cs.u);
         k_.c0 = (T)std::sqrt(cs.gamma * (cs.P / cs.rho));
+        k_.roe = cs.flux_solver == FV2D_ROE;
 
         FV2D_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
         // ---- arena layout

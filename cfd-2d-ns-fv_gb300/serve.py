@@ -42,6 +42,7 @@ class Record:
     stalled: bool = False
     failed: bool = False
     state: object = None
+    stage_bytes: float = 0.0
 
 
 class Progress:
@@ -113,16 +114,22 @@ def _percentiles(vals):
 
 
 def serve(batch, stream, pool, duration, target=1e-6, max_iters=2000, check_every=25, clock=time.monotonic,
-          sleep=time.sleep, keep_states=False, records_out=None, stall_iters=0, stall_gain=0.01):
+          sleep=time.sleep, keep_states=False, records_out=None, stall_iters=0, stall_gain=0.01,
+          stage_bytes=None):
     """Continuous batching over `stream` [(arrival s, spec)] for `duration` seconds.  With
     keep_states the final state of every retired solve is kept on its record (records_out).
-    stall_iters > 0 also retires solves whose residual stopped dropping (Progress)."""
+    stall_iters > 0 also retires solves whose residual stopped dropping (Progress).
+    stage_bytes(grid, spec): algorithmic bytes of one RK stage of a request, summed over the
+    stages run into `bytes_per_s`.
+    Time in service (admission to retirement) is reported apart from the queue wait (arrival to
+    admission); time-to-converge is their sum."""
     t0 = clock()
     pending = deque()
     active = {}                # sid -> (record, r0 or None)
     records = []
     idx = 0
     cell_stages = 0.0
+    nbytes = 0.0
     max_queue = 0
     steps = 0
     active_sum = 0
@@ -144,6 +151,7 @@ def serve(batch, stream, pool, duration, target=1e-6, max_iters=2000, check_ever
             steps += 1
             active_sum += len(active)
             cell_stages += 3.0 * check_every * sum(a[0].cells for a in active.values())
+            nbytes += 3.0 * check_every * sum(a[0].stage_bytes for a in active.values())
         admitted = 0
         while pending:                                   # FIFO admission while the arena has room
             rec, spec = pending[0]
@@ -156,6 +164,8 @@ def serve(batch, stream, pool, duration, target=1e-6, max_iters=2000, check_ever
                     break
                 raise
             rec.admit = clock() - t0
+            if stage_bytes is not None:
+                rec.stage_bytes = float(stage_bytes(pool.grids[pool.index_for(spec["cells"])], spec))
             active[sid] = [rec, Progress(target, stall_iters, stall_gain)]
             pending.popleft()
             admitted += 1
@@ -195,13 +205,18 @@ def serve(batch, stream, pool, duration, target=1e-6, max_iters=2000, check_ever
     ttc = [r.finish - r.arrival for r in finished]
     p50, p99 = _percentiles(ttc)
     w50, w99 = _percentiles([r.admit - r.arrival for r in records if r.admit >= 0])
+    s50, s99 = _percentiles([r.finish - r.admit for r in finished])
     return dict(mode="continuous batching", duration_s=round(elapsed, 2), arrived=len(records), admitted=sum(r.admit >= 0 for r in records),
                 completed=len(finished), converged=sum(r.converged for r in finished), stalled=sum(r.stalled for r in finished),
                 failed=sum(r.failed for r in finished), failed_requests=[r.rid for r in finished if r.failed][:32],
                 in_flight=len(active), queued=len(pending), max_queue=max_queue,
                 mean_active=round(active_sum / steps, 1) if steps else 0,
-                ttc_p50_s=p50, ttc_p99_s=p99, wait_p50_s=w50, wait_p99_s=w99,
+                ttc_p50_s=p50, ttc_p99_s=p99, wait_p50_s=w50, wait_p99_s=w99, service_p50_s=s50, service_p99_s=s99,
+                retired_by={"converged": sum(r.converged for r in finished), "stalled": sum(r.stalled for r in finished),
+                            "max_iters": sum(not (r.converged or r.stalled or r.failed) for r in finished),
+                            "failed": sum(r.failed for r in finished)},
                 cell_stage_per_s=cell_stages / elapsed if elapsed > 0 else 0.0,
+                bytes_per_s=nbytes / elapsed if elapsed > 0 and stage_bytes is not None else None,
                 target=target, max_iters=max_iters, check_every=check_every, stall_iters=stall_iters)
 
 

@@ -25,7 +25,7 @@ extern "C" {
 #define FV2D_ERR_ARG        1   /* invalid argument or handle                                   */
 #define FV2D_ERR_IO         2   /* input.in / grid file could not be opened or parsed           */
 #define FV2D_ERR_MESH       3   /* mesh rejected (ids out of range, unsupported ordering)       */
-#define FV2D_ERR_CASE       4   /* option the solver step does not implement (ROE, MINMOD, ...) */
+#define FV2D_ERR_CASE       4   /* option the solver step does not implement (order 3, ...)     */
 #define FV2D_ERR_CUDA       5   /* CUDA runtime error                                           */
 #define FV2D_ERR_NOMEM      6   /* device memory exhausted                                      */
 #define FV2D_ERR_STATE      7   /* non-physical state detected (NaN, rho <= 0 or P <= 0)        */
@@ -38,6 +38,9 @@ extern "C" {
 #define FV2D_EULER 1
 #define FV2D_NS 2
 #define FV2D_RUSANOV 1
+/* ROE is run as the reference runs it: its res() calls no flux routine (res.cpp:62-69), so every
+ * face's inviscid flux is class_F::init's -101 (class_f.hpp:26-30) and the time step keeps the
+ * initial spectral terms (class_q.hpp:61-62); only the NS viscous flux is computed.             */
 #define FV2D_ROE 2
 #define FV2D_LIM_NONE 0
 #define FV2D_LIM_MINMOD 1
@@ -221,20 +224,30 @@ void* fv2d_batch_stream(fv2d_batch* b);
  * solution_poly_order = 0, src/solver/res.cpp:21: boundary ghosts, Rusanov flux, gather / volume;
  * no viscous flux, as in the reference at first order) and allocates nothing.
  *
- * Its per-face scratch is a static device array of FV2D_NOALLOC_MAX_FACES x 4 doubles (8 MiB),
- * held by every GPU that loads this library until the process exits; meshes with more faces are
- * rejected with FV2D_ERR_ARG (use fv2d_create / fv2d_stage for those).  The first call on each
- * device looks up that array's device address with the device current; make that first call
- * before any stream capture.  The scratch is fully rewritten before it is read, so no state
+ * Its per-face scratch is a static device array of FV2D_NOALLOC_MAX_FACES x 4 doubles (8 MiB)
+ * that lives with the library's device code on each GPU until the process exits; meshes with more
+ * faces are rejected with FV2D_ERR_ARG (use fv2d_create / fv2d_stage for those).  The first call on
+ * each device looks up that array's device address with the device current; make that first call
+ * before any stream capture.  Under CUDA's lazy module loading (the default; CUDA_MODULE_LOADING
+ * unset or LAZY) the library's device code and this array are only placed on a device by that first
+ * call, so the FIRST call does take device memory: a host whose allocator reserves the GPU's memory
+ * makes one warm-up call per device (any small mesh) before it reserves its pool, or runs with
+ * CUDA_MODULE_LOADING=EAGER.  Every later call allocates nothing.  The looked-up address belongs to
+ * the device's primary context: resetting the device (cudaDeviceReset) after the first call is not
+ * supported in the same process.  The scratch is fully rewritten before it is read, so no state
  * carries over between calls, but all calls share it: calls that overlap on the GPU (other
  * streams, other host threads on the same device) race and must be serialised by the caller.
  * The kernels are launched on `stream` (a cudaStream_t, NULL = legacy default stream) and the call
  * returns without waiting; errors: fv2d_last_error(NULL).
  *
- * Mesh arrays use the reference's numbering and codes (0-based; face_cell2 < 0 is the BC code
- * -1..-4), cell_faces holds (face id << 1) | side (side 1 when the cell is face_cell2) in
+ * Mesh arrays use the reference's numbering and codes, 0-based, and must be in range (they are
+ * not checked on the device): face_cell1 in [0, num_cells); face_cell2 in [0, num_cells) for an
+ * interior face or one of the BC codes -1 (FREESTREAM), -2 (SLIP_WALL), -3 (EXTRAPOLATION),
+ * -4 (NO_SLIP_WALL); cell_face_offsets non-decreasing from 0; cell_faces holds
+ * (face id << 1) | side (side 1 when the cell is face_cell2) with face ids in [0, num_faces), in
  * ascending face id per cell, which reproduces the reference's summation order; q and r are SoA
- * p1..p4 blocks of num_cells doubles.  From the case only gamma and the [init] state are read. */
+ * p1..p4 blocks of num_cells doubles.  From the case only gamma, the [init] state and
+ * flux_solver are read (RUSANOV only: ROE is rejected with FV2D_ERR_CASE). */
 #define FV2D_NOALLOC_MAX_FACES 262144
 typedef struct fv2d_noalloc_mesh {
     int num_cells, num_faces;

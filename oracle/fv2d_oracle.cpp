@@ -762,7 +762,10 @@ int copy_out(const vd& a, double* out, int off) {
 
 Oracle* finish_open(Oracle* o, const vi& fp1, const vi& fp2, const vi& fc1, const vi& fc2) {
     if (o->cs.order != 1 && o->cs.order != 2) { delete o; return nullptr; }
-    if (o->cs.flux_solver != 1) { delete o; return nullptr; }
+    /* RUSANOV (1) or ROE (2): with ROE the reference's res() calls no flux routine (res.cpp:62-69), so
+     * the inviscid flux keeps class_F::init's -101 (class_f.hpp:26-30) and Vn_avg / c_avg keep their
+     * initial values (class_q.hpp:61-62); res() above reproduces both by skipping the Rusanov block */
+    if (o->cs.flux_solver != 1 && o->cs.flux_solver != 2) { delete o; return nullptr; }
     for (int f = 0; f < o->m.nf; f++) {
         if (fc1[f] < 1 || fc1[f] > o->m.nc || fc2[f] < -1 || fc2[f] > o->m.nc ||
             fp1[f] < 1 || fp1[f] > o->m.np || fp2[f] < 1 || fp2[f] > o->m.np) { delete o; return nullptr; }

@@ -98,7 +98,8 @@ def _ip(a):
 def case_struct(c: dict) -> FvoCase:
     lim = {"NONE": 0, "MINMOD": 1, "SQUEEZE": 2}[c["limiter"]]
     codes = {"FREESTREAM": -1, "SLIP_WALL": -2, "EXTRAPOLATION": -3, "NO_SLIP_WALL": -4}
-    return FvoCase(int(c["solution_poly_order"]) + 1, 1 if c["eqn"] == "EULER" else 2, 1, lim,
+    flux = 1 if c.get("flux_solver", "RUSANOV") == "RUSANOV" else 2
+    return FvoCase(int(c["solution_poly_order"]) + 1, 1 if c["eqn"] == "EULER" else 2, flux, lim,
                    1 if c["time_step_type"] == "GLOBAL" else 2, 2, codes[c["BC1"]], codes[c["BC2"]],
                    float(c["CFL"]), float(c["gamma"]), float(c["R"]), float(c["mu"]), float(c["Pr"]),
                    float(c["P"]), float(c["rho"]), float(c["u"]), float(c["v"]))

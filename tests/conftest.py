@@ -10,6 +10,15 @@ sys.path.insert(0, ROOT)
 import __graft_entry__ as entry  # noqa: E402
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+
+def golden_names(long=False):
+    """Golden fixture names: per-stage cases, or (long=True) the whole-run cases long_*.npz."""
+    import glob
+    names = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+    return [n for n in names if n.startswith("long_") == long]
+
+
 REFERENCE_TREE = entry.REFERENCE_TREE
 
 

@@ -6,8 +6,12 @@ by oracle/Makefile) on small cases and stores, per case:
   - per RK stage: SHA-256 of the exact FP64 bytes of the residual, Q*, Qbar and dt (file order,
     SoA), and for small meshes the arrays themselves,
   - SHA-256 of the reference geometry arrays.
+Long-horizon cases (files named long_*.npz) store, instead of every stage, the SHA-256 of Qbar and
+the residual after whole SSP-RK3 iterations (ssp_rk3() called as main.cpp:121-133 calls it) at a
+list of checkpoints.
 The GPU parity tests replay the same mesh and options and must reproduce these bytes.
-Run here (where the reference tree exists):  python tests/golden/make_golden.py
+Run where the reference tree exists (FV2D_REFERENCE, default /root/reference):
+    python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
@@ -24,7 +28,8 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 import __graft_entry__ as entry  # noqa: E402
 
-REF_GRIDS = "/root/reference/grids"
+REF_TREE = os.environ.get("FV2D_REFERENCE", "/root/reference")
+REF_GRIDS = os.path.join(REF_TREE, "grids")
 FULL_ARRAYS_MAX_CELLS = 200
 GEOM_NAMES = ["area", "nx", "ny", "fcx", "fcy", "c1dx", "c1dy", "c2dx", "c2dy", "dxj", "dyj", "dist", "lx", "ly",
               "mx", "my", "vol", "ccx", "ccy", "Ixx", "Iyy", "Ixy", "delta"]
@@ -40,6 +45,9 @@ def cases(mg):
     ch128 = mg.channel_bump_quads(128, 64)
     simple = mg.read_grid(os.path.join(REF_GRIDS, "simple_grid.in"), "simple_grid")
     airfoil = mg.read_grid(os.path.join(REF_GRIDS, "grid_file.in"), "airfoil")
+    # a Voronoi bump channel with 4-6-sided cells (the reference's reader takes at most 6 sides)
+    vor = mg.voronoi_bump_channel(3000, seed=3, jitter=0.15)
+    m07 = mg.mach_speed(0.7)
     ns = dict(eqn="NS", mu=0.5, Pr=0.72)
     return [
         ("ch16_euler_sq_global", ch16, dict(eqn="EULER", limiter="SQUEEZE", time_step_type="GLOBAL", CFL=0.8,
@@ -65,7 +73,36 @@ def cases(mg):
                                                   CFL=0.8, BC1="SLIP_WALL", BC2="FREESTREAM", u=170.147), 6, None),
         ("channel128_euler_sq_global", ch128, dict(eqn="EULER", limiter="SQUEEZE", time_step_type="GLOBAL",
                                                    CFL=0.8, BC1="SLIP_WALL", BC2="FREESTREAM", u=m05), 15, None),
+        ("vor3k_euler_sq_global", vor, dict(eqn="EULER", limiter="SQUEEZE", time_step_type="GLOBAL", CFL=0.8,
+                                            BC1="SLIP_WALL", BC2="FREESTREAM", u=m07), 12, None),
+        ("vor3k_ns_sq_local_noslip", vor, dict(ns, mu=0.05, limiter="SQUEEZE", time_step_type="LOCAL", CFL=0.9,
+                                               BC1="NO_SLIP_WALL", BC2="FREESTREAM", u=m07), 12, None),
+        # flux_solver = ROE: the reference's res() computes no inviscid flux (res.cpp:62-69)
+        ("ch16_ns_roe_sq_local", ch16, dict(ns, flux_solver="ROE", limiter="SQUEEZE", time_step_type="LOCAL",
+                                            CFL=0.5, BC1="NO_SLIP_WALL", BC2="FREESTREAM", u=m05), 9, None),
+        ("ch16_euler_roe_order0", ch16, dict(eqn="EULER", flux_solver="ROE", solution_poly_order=0,
+                                             limiter="NONE", time_step_type="GLOBAL", CFL=0.1, BC1="SLIP_WALL",
+                                             BC2="FREESTREAM", u=m05), 9, None),
     ]
+
+
+def long_cases(mg):
+    """(name, grid, options, iteration checkpoints): whole runs of the driver loop."""
+    m05 = mg.mach_speed(0.5)
+    # the plain FP64 method as the benchmark configuration states it: 128x64 quads of a 3 x 1 channel
+    # with a 10 %-thick circular-arc bump, Euler, second order, squeeze, GLOBAL dt at CFL 0.8,
+    # Mach 0.5, slip walls and freestream inlet/outlet, 2000 iterations
+    return [
+        ("long_c1_channel128_euler_sq_global", mg.channel_bump_quads(128, 64),
+         dict(eqn="EULER", limiter="SQUEEZE", time_step_type="GLOBAL", CFL=0.8, BC1="SLIP_WALL", BC2="FREESTREAM",
+              u=m05, nmax=2000), [1, 10, 100, 500, 2000]),
+    ]
+
+
+def stable(case):
+    """The case as stored: the grid path (a temporary file) reduced to its name, so that
+    regenerating the fixtures reproduces their bytes."""
+    return dict(case, grid_file=os.path.basename(case["grid_file"]))
 
 
 def restart_state(grid, case, seed):
@@ -83,7 +120,7 @@ def restart_state(grid, case, seed):
 def main():
     pkg = entry.load_package()
     orc = entry.load_oracle()
-    orc.build(ref_dir="/root/reference")
+    orc.build(ref_dir=REF_TREE)
     assert orc.available("ref"), "reference harness not built"
     mg = pkg.meshgen
     tmp = tempfile.mkdtemp()
@@ -95,7 +132,7 @@ def main():
         case = mg.write_input(ipath, grid_file=gpath, **opts)
         ref = orc.Oracle("ref", ipath)
         out = dict(x=grid.x, y=grid.y, fp1=grid.fp1, fp2=grid.fp2, fc1=grid.fc1, fc2=grid.fc2,
-                   num_cells=np.int64(grid.num_cells), case_json=np.array(json.dumps(case)),
+                   num_cells=np.int64(grid.num_cells), case_json=np.array(json.dumps(stable(case))),
                    nstages=np.int64(nstages))
         if restart_seed is not None:
             q0 = restart_state(grid, case, restart_seed)
@@ -123,6 +160,22 @@ def main():
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
         manifest[name] = dict(cells=grid.num_cells, faces=grid.num_faces, stages=nstages, options=opts)
         print(name, grid.num_cells, "cells", nstages, "stages")
+    for name, grid, opts, checkpoints in long_cases(mg):
+        gpath = os.path.join(tmp, name + ".grid")
+        mg.write_grid(gpath, grid)
+        ipath = os.path.join(tmp, name + ".in")
+        case = mg.write_input(ipath, grid_file=gpath, **opts)
+        ref = orc.Oracle("ref", ipath)
+        recs, done = [], 0
+        for n in checkpoints:
+            ref.iterate(n - done)
+            done = n
+            recs.append({"iter": n, "qbar": sha(ref.get(orc.QBAR)), "res": sha(ref.get(orc.RES))})
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), x=grid.x, y=grid.y, fp1=grid.fp1, fp2=grid.fp2,
+                            fc1=grid.fc1, fc2=grid.fc2, num_cells=np.int64(grid.num_cells),
+                            case_json=np.array(json.dumps(stable(case))), iter_hashes=np.array(json.dumps(recs)))
+        manifest[name] = dict(cells=grid.num_cells, faces=grid.num_faces, iterations=checkpoints, options=opts)
+        print(name, grid.num_cells, "cells", checkpoints[-1], "iterations")
     with open(os.path.join(HERE, "MANIFEST.json"), "w") as fh:
         json.dump(manifest, fh, indent=1, sort_keys=True)
 

@@ -1,7 +1,6 @@
 """FP64 GPU path against the reference (golden fixtures, replayed byte for byte) and against the
 oracle port on meshes the reference cannot read (7-9-sided cells).  All calls go through the
 C ABI (ctypes)."""
-import glob
 import hashlib
 import json
 import os
@@ -9,11 +8,12 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, bits_equal, max_rel, wheels_grid
+from conftest import GOLDEN, golden_names, bits_equal, max_rel, wheels_grid
 
 pytestmark = pytest.mark.gpu
 
-CASES = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+CASES = golden_names()
+LONG = golden_names(long=True)
 TOL = 1e-12   # relative, per value: the FP64 path's parity bar (it is expected to be bit-exact)
 
 
@@ -56,6 +56,48 @@ def test_fp64_reproduces_reference_every_stage(name, pkg, orc):
         if "qstar" in rec:
             assert sha(gpu.get(1)) == rec["qstar"], f"stage {s}: Q* not bit-identical"
     assert bits_equal(gpu.get_state(), z["final_qbar"])
+    gpu.close()
+
+
+@pytest.mark.parametrize("name", LONG)
+def test_fp64_full_run_reproduces_reference(name, pkg):
+    """The plain FP64 method run as the reference's driver runs it (ssp_rk3() once per iteration,
+    main.cpp:121-133; here fv2d_step, i.e. graph-replayed iterations): Qbar and the residual after
+    1, 10, 100, 500 and 2000 iterations are the reference's exact bytes."""
+    z, grid, case = load(name, pkg)
+    gpu = pkg.Solver(grid, case, precision=pkg.FP64)
+    done = 0
+    for rec in json.loads(str(z["iter_hashes"])):
+        gpu.step(rec["iter"] - done)
+        done = rec["iter"]
+        assert sha(gpu.get_state()) == rec["qbar"], f"Qbar not bit-identical after iteration {done}"
+        assert sha(gpu.get(2)) == rec["res"], f"residual not bit-identical after iteration {done}"
+    gpu.close()
+
+
+def test_fp64_long_run_cylinder_vs_oracle(pkg, orc):
+    """300 iterations of the benchmark's flow (NS cylinder of diameter 1, Re 100, Mach 0.2, Pr 0.72,
+    no-slip cylinder, freestream box, squeeze, LOCAL dt at CFL 0.5) on a 12k-cell Voronoi mesh of an
+    8 x 4 box with 4-8-sided cells, bit for bit against the oracle at iterations 1, 30 and 300: past
+    the start-up transient, where the limiter's warp-shared quotient path is taken or left per warp
+    as the flow settles."""
+    mg = pkg.meshgen
+    g = mg.voronoi_cylinder(12000, seed=0, box=(8.0, 4.0), h_wall=0.01, h_far=0.08)
+    u = mg.mach_speed(0.2)
+    case = dict(mg.DEFAULT_CASE, eqn="NS", mu=1.225 * u * 1.0 / 100.0, Pr=0.72, u=u, v=0.0, limiter="SQUEEZE",
+                time_step_type="LOCAL", CFL=0.5, BC1="NO_SLIP_WALL", BC2="FREESTREAM", solution_poly_order=1)
+    gpu = pkg.Solver(g, case, precision=pkg.FP64)
+    port = orc.Oracle("port", grid=g, case=case)
+    done = 0
+    for n in (1, 30, 300):
+        gpu.step(n - done)
+        port.iterate(n - done)
+        done = n
+        assert bits_equal(gpu.get_state(), port.get(orc.QBAR)), f"Qbar after iteration {n}"
+        assert bits_equal(gpu.get(2), port.get(orc.RES)), f"residual after iteration {n}"
+        assert bits_equal(gpu.get(3), port.get(orc.DT)), f"dt after iteration {n}"
+        assert bits_equal(gpu.get(4), port.get(orc.QBAR_GRAD)), f"Qbar gradient after iteration {n}"
+    assert np.all(np.isfinite(gpu.get_state()))
     gpu.close()
 
 

@@ -1,7 +1,6 @@
 """Host side of the library (no GPU): C-ABI exports, input.in and grid parsing, connectivity, BC
 tagging, geometry (bit-exact against the reference) and the renumbering."""
 import ctypes
-import glob
 import hashlib
 import json
 import os
@@ -11,9 +10,9 @@ import tempfile
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, ROOT, bits_equal
+from conftest import GOLDEN, ROOT, bits_equal, golden_names
 
-CASES = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+CASES = golden_names()
 
 
 def sha(a):
@@ -157,11 +156,13 @@ def test_mesh_errors(pkg):
     with pytest.raises(pkg.Fv2dError) as e:
         pkg.HostMesh(late, ns)
     assert e.value.code == 3
-    for opts in (dict(flux_solver="ROE"), dict(solution_poly_order=2), dict(time_step_type="LOCAL", CFL=-1.0)):
+    for opts in (dict(solution_poly_order=2), dict(time_step_type="LOCAL", CFL=-1.0)):
         c = pkg.case_from_dict(dict(pkg.meshgen.DEFAULT_CASE, **opts))
         with pytest.raises(pkg.Fv2dError) as e:
             pkg.HostMesh(g, c)
         assert e.value.code == 4
+    # ROE is accepted and run as the reference runs it (no inviscid flux routine, res.cpp:62-69)
+    pkg.HostMesh(g, pkg.case_from_dict(dict(pkg.meshgen.DEFAULT_CASE, flux_solver="ROE"))).close()
 
 
 def test_fp64_engine_is_built_without_fma_contraction():

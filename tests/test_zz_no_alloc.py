@@ -1,7 +1,9 @@
 """fv2d_residual_noalloc: the first-order residual for callers that cannot allocate device memory
 (their inputs and outputs live in memory they already own; the call's face scratch is a static
 device array).  Checked through the C ABI against the existing entry point (a solver handle's
-first stage, fv2d_stage) on two calls in a row, to the FP64 parity tolerance."""
+first stage, fv2d_stage) on two calls in a row, to the FP64 parity tolerance; the device's free
+memory is the same before and after a call that follows the first; a mesh of exactly the face
+limit runs."""
 import ctypes
 
 import numpy as np
@@ -87,13 +89,86 @@ def test_residual_noalloc_matches_existing_entry_point_twice(pkg):
         r_dev.fill_(float("nan"))
         cs = pkg.case_from_dict(case)
         torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
         rc = fn(ctypes.byref(m), ctypes.byref(cs), q_dev.data_ptr(), r_dev.data_ptr(), None)
         assert rc == 0, lib.fv2d_last_error(None)
         torch.cuda.synchronize()
+        if call > 0:   # the first call may place the library's code and scratch (lazy module loading)
+            assert torch.cuda.mem_get_info()[0] == free0, "a call after the first took device memory"
         r = r_dev.cpu().numpy()
         ref = residual_existing(pkg, grid, case, q)
         assert np.all(np.isfinite(r))
         assert max_rel(r, ref, floor=1e-30) <= TOL, f"call {call}: max rel {max_rel(r, ref, floor=1e-30):.3e}"
+
+
+def split_quads(pkg, grid, k):
+    """`grid` with its first k quadrilateral cells each cut into two triangles along a diagonal: k
+    more cells and k more (interior) faces, appended after the existing ones.  The new face's c1 is
+    the triangle on its left (the face normal points out of c1), as the grid format requires."""
+    fp1, fp2 = grid.fp1.astype(np.int64).copy(), grid.fp2.astype(np.int64).copy()
+    fc1, fc2 = grid.fc1.astype(np.int64).copy(), grid.fc2.astype(np.int64).copy()
+    x, y = grid.x, grid.y
+    faces_of = {}
+    for f in range(grid.num_faces):
+        for c in (fc1[f], fc2[f]):
+            if c > 0:
+                faces_of.setdefault(int(c), []).append(f)
+    nf, nc = grid.num_faces, grid.num_cells
+    new_faces = []
+    for c in range(1, k + 1):
+        fs = faces_of[c]
+        assert len(fs) == 4
+        adj = {}
+        for f in fs:
+            adj.setdefault(fp1[f], []).append(fp2[f])
+            adj.setdefault(fp2[f], []).append(fp1[f])
+        loop = [fp1[fs[0]], fp2[fs[0]]]
+        while len(loop) < 4:
+            a, b = adj[loop[-1]]
+            loop.append(a if a != loop[-2] else b)
+        p0, p1, p2, p3 = loop
+        nc += 1
+        for f in fs:   # the edges of triangle (p2, p3, p0) move to the new cell
+            if {fp1[f], fp2[f]} in ({p2, p3}, {p3, p0}):
+                if fc1[f] == c:
+                    fc1[f] = nc
+                else:
+                    fc2[f] = nc
+        dx, dy = x[p2 - 1] - x[p0 - 1], y[p2 - 1] - y[p0 - 1]
+        left_is_t1 = dx * (y[p1 - 1] - y[p0 - 1]) - dy * (x[p1 - 1] - x[p0 - 1]) > 0
+        new_faces.append((p0, p2, c if left_is_t1 else nc, nc if left_is_t1 else c))
+    a = np.array(new_faces, dtype=np.int64)
+    cat = lambda u, v: np.concatenate([u, v]).astype(np.int32)  # noqa: E731
+    return pkg.meshgen.Grid(x, y, cat(fp1, a[:, 0]), cat(fp2, a[:, 1]), cat(fc1, a[:, 2]), cat(fc2, a[:, 3]), nc,
+                            f"{grid.name}_split{k}")
+
+
+def test_residual_noalloc_at_the_face_limit(pkg):
+    """A mesh of exactly FV2D_NOALLOC_MAX_FACES faces: the last face's contribution lands in the
+    scratch array's last entries and the residual equals the existing entry point's."""
+    torch = pytest.importorskip("torch")
+    lib = pkg.library()
+    fn = lib.fv2d_residual_noalloc
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.POINTER(NoallocMesh), ctypes.POINTER(pkg.Case), ctypes.c_void_p, ctypes.c_void_p,
+                   ctypes.c_void_p]
+    base = pkg.meshgen.channel_bump_quads(512, 255)                # 261,887 faces
+    grid = split_quads(pkg, base, 262144 - base.num_faces)
+    assert grid.num_faces == 262144
+    case = dict(pkg.meshgen.DEFAULT_CASE, solution_poly_order=0, limiter="NONE", eqn="EULER", BC1="SLIP_WALL",
+                BC2="FREESTREAM", u=pkg.meshgen.mach_speed(0.5), v=10.0)
+    m, keep = device_mesh(pkg, torch, grid, case)
+    q = perturbed_state(case, grid.num_cells, seed=7)
+    q_dev = torch.from_numpy(q).cuda()
+    r_dev = torch.full((4 * grid.num_cells,), float("nan"), dtype=torch.float64, device="cuda")
+    cs = pkg.case_from_dict(case)
+    rc = fn(ctypes.byref(m), ctypes.byref(cs), q_dev.data_ptr(), r_dev.data_ptr(), None)
+    assert rc == 0, lib.fv2d_last_error(None)
+    torch.cuda.synchronize()
+    r = r_dev.cpu().numpy()
+    ref = residual_existing(pkg, grid, case, q)
+    assert np.all(np.isfinite(r))
+    assert max_rel(r, ref, floor=1e-30) <= TOL
 
 
 def test_residual_noalloc_rejects_oversized_mesh(pkg):
