@@ -38,14 +38,15 @@ def _units():
     return [
         # (source, object, command prefix)
         ("fv2d_host.cpp", host),
+        ("fv2d_tiles.cpp", host),
         ("fv2d_output.cpp", host),
         ("fv2d_api.cu", [nvcc] + common),
         # the FP64 engine must not contract a*b+c: bit-identical with the reference
         ("fv2d_fp64.cu", [nvcc] + common + ["-fmad=false"]),
-        # nor the FP32 engine: its kernels are memory-bound, and without contraction every kernel
-        # that runs the shared per-element code (single solve, batch) rounds identically; its
-        # divisions and square roots use the approximate (few-ulp) forms
-        ("fv2d_fp32.cu", [nvcc] + common + ["-fmad=false", "-prec-div=false", "-prec-sqrt=false"]),
+        # the FP32 engine: a single solve and a batch run the same fused stage kernels, so FMA
+        # contraction is allowed (both round alike); divisions and square roots use the
+        # approximate (few-ulp) forms
+        ("fv2d_tiled.cu", [nvcc] + common + ["-prec-div=false", "-prec-sqrt=false"]),
         ("fv2d_noalloc.cu", [nvcc] + common + ["-fmad=false"]),
     ]
 

@@ -24,7 +24,7 @@ struct NvtxRange {
 
 namespace fv2d {
 const char* const kKernelNames[K_COUNT] = {"k_gradient", "k_face", "k_update", "k_spectral_init",
-                                          "k_state_in", "k_state_out", "k_res_norm_partial"};
+                                          "k_state_in", "k_state_out", "k_res_norm_partial", "k_tstage"};
 }
 
 struct fv2d_handle {
@@ -451,6 +451,7 @@ void* fv2d_batch_stream(fv2d_batch* b) { return (b && b->b) ? b->b->stream() : n
 
 namespace fv2d {
 void batch_footprint(int precision, long long cells, long long faces, long long incs, long long* bytes) {
+    if (precision == FV2D_FP32) { tiled_footprint(cells, faces, bytes); return; }
     const long long s = precision == FV2D_FP64 ? 8 : 4;
     const long long cell = (precision == FV2D_FP64 ? 9 : 11) * 4 * s + 4 * s + 24 + 4;   // Q[3], G[3], (D, lo), dt, S, vol, 1/vol, LSQ, offsets
     const long long face = 3 * 4 + 15 * s + 4 * s + s         // ids, geometry (+ 1/|dist|), contribution, spectral term

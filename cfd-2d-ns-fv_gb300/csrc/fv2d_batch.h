@@ -43,5 +43,7 @@ Batch* make_batch_fp32();
 
 // Device bytes a solve occupies: per cell, per face, per incidence (both precisions).
 void batch_footprint(int precision, long long cells, long long faces, long long incs, long long* bytes);
+// The FP32 engine's allowance for a solve of `cells` cells and `faces` faces (its tile layout).
+void tiled_footprint(long long cells, long long faces, long long* bytes);
 
 }  // namespace fv2d

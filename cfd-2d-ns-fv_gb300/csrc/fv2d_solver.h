@@ -9,7 +9,8 @@
 
 namespace fv2d {
 
-enum KernelId { K_GRADIENT = 0, K_FACE, K_UPDATE, K_SPECTRAL, K_STATE_IN, K_STATE_OUT, K_NORM, K_COUNT };
+// K_TSTAGE: the FP32 engine's fused stage kernel (gradient, flux and update of a tile in one launch)
+enum KernelId { K_GRADIENT = 0, K_FACE, K_UPDATE, K_SPECTRAL, K_STATE_IN, K_STATE_OUT, K_NORM, K_TSTAGE, K_COUNT };
 extern const char* const kKernelNames[K_COUNT];
 
 class Solver {

@@ -1,0 +1,574 @@
+// Device code of the FP32 engine: one fused kernel per SSP-RK3 stage over the tile layout of
+// fv2d_tiles.h.  Each CTA takes tiles from a counter; per tile:
+//   load    one thread arms an mbarrier and issues bulk asynchronous copies (cp.async.bulk, the
+//           TMA engine) of the tile's record block, csr block, halo list and core-cell states into
+//           shared memory; every wait on the mbarrier is bounded and reports a timeout
+//   gather  the states of the ring-1 and ring-2 cells (L2-resident neighbours of the tile)
+//   grad    LSQ gradient + squeeze limiter of every core and ring-1 cell (compute_gradient,
+//           src/solver/cell_gradient.cpp:9-131; squeeze, src/solver/squeeze.cpp:9-155), each cell's
+//           sums in ascending original face id; limited gradients stay in shared memory
+//   flux    reconstruction + boundary ghosts (reconstruction.cpp:22-80), NS face terms (:86-164),
+//           Rusanov flux (rusanov.cpp:20-36) of every face of a core cell; the face's contribution
+//           V*A - F*A (res.cpp:81-89) overwrites its geometry rows in shared memory
+//   update  residual gather (res.cpp:74-109), time step (ssp_rk3.cpp:24-47) and the SSP-RK3 stage
+//           (ssp_rk3.cpp:50-77) of the core cells, in the compensated delta form of the FP32 path
+// A face shared by two tiles is evaluated by both, with the same inputs and the same code, so both
+// get the same value; every per-cell sum runs in a fixed order, so results do not depend on the
+// tile schedule, and a solve gives the same bits alone and in a batch (both run these kernels).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "fv2d_kernels.cuh"
+#include "fv2d_tiles.h"
+
+namespace fv2d {
+
+struct TParams {   // per solve
+    Consts<float> k;
+    int order2, ns, squeeze, global_dt;
+    int fresh, init_prims, pad0, pad1;
+};
+
+struct TArgs {
+    const TileDesc* tiles;
+    const int* ntiles;
+    int* counter;              // [3] next tile of each stage kernel (zeroed before each iteration)
+    TParams* P;
+    const uint32_t* rec;
+    const uint16_t* csr;
+    const int* halo;
+    const int* qcell;
+    Q4<float>* Q[3];           // stage inputs: Qn, Q1, Q2
+    Q4<float>* G[3];           // limited gradient of each stage input (x, y per cell)
+    Q4<float>* D;              // RK increment (delta form)
+    Q4<float>* Qlo;            // compensation term of Qn
+    Q4<float>* R;              // residual (null: not kept)
+    float *dt, *S;
+    const float *vol, *rvol;
+    const double *Ixx, *Iyy, *Ixy;
+    float* smax;               // [solves] max spectral sum (GLOBAL dt)
+    int* flags;                // [solves] non-physical state seen
+    double* tpart;             // [tiles][4] residual sums of squares of the last stage (null: none)
+    int* err;                  // bit 1: an mbarrier wait timed out; bit 2: a tile descriptor out of range
+    int store_r;               // keep R on stages 0 and 1 too
+};
+
+// Shared-memory plan of one CTA (bytes; every region 16-byte aligned).
+constexpr int kSmRecWords = 5 * kTileRecs + 3 * kTileGeo;
+constexpr int kSmRec = 4 * kSmRecWords;
+constexpr int kSmCsr = ((2 * kTileCsr + 15) / 16) * 16;
+constexpr int kSmHalo = 4 * kTileCells;
+constexpr int kSmCq = 16 * kTileCells;
+constexpr int kSmCg = 32 * kTileGrad;
+constexpr int kSmTotal = kSmRec + kSmCsr + kSmHalo + kSmCq + kSmCg;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint32_t mb, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mb), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t mb, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(bytes) : "memory");
+}
+// Bounded wait for the mbarrier phase with the given parity: false after ~2^22 polls (each poll
+// suspends the thread for a while, so this is far longer than any copy takes).
+__device__ __forceinline__ bool mbar_wait(uint32_t mb, uint32_t parity) {
+    for (int i = 0; i < (1 << 22); i++) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(mb), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+// Bulk copy global -> shared (16-byte aligned addresses, size a multiple of 16), completing on mb.
+__device__ __forceinline__ void tma_load(void* dst, const void* src, uint32_t bytes, uint32_t mb) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(mb)
+                 : "memory");
+}
+
+__device__ __forceinline__ float fw(uint32_t w) { return __uint_as_float(w); }
+
+// Primitives of a conservative state; returns 1/rho for later quotients.
+__device__ __forceinline__ void tprims(const float p[4], const Consts<float>& k, float& rho, float& u, float& v,
+                                       float& P, float& y) {
+    rho = p[0];
+    y = 1.0f / rho;
+    u = p[1] * y;
+    v = p[2] * y;
+    P = (p[3] - 0.5f * rho * (u * u + v * v)) * k.gm1;
+}
+
+template <int STAGE>
+__global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
+    extern __shared__ __align__(128) unsigned char sm[];
+    uint32_t* srec = reinterpret_cast<uint32_t*>(sm);
+    uint16_t* scsr = reinterpret_cast<uint16_t*>(sm + kSmRec);
+    int* shalo = reinterpret_cast<int*>(sm + kSmRec + kSmCsr);
+    Q4<float>* cq = reinterpret_cast<Q4<float>*>(sm + kSmRec + kSmCsr + kSmHalo);
+    Q4<float>* cg = reinterpret_cast<Q4<float>*>(sm + kSmRec + kSmCsr + kSmHalo + kSmCq);
+    __shared__ TileDesc td;
+    __shared__ TParams tp;
+    __shared__ __align__(8) unsigned long long mbar;
+    __shared__ int s_tile;
+    __shared__ float redf[kTileCore / 32];
+    __shared__ double redd[4][kTileCore / 32];
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t mb = smem_u32(&mbar);
+    if (tid == 0) mbar_init(mb, 1);
+    __syncthreads();
+    uint32_t parity = 0;
+    const int ntiles = *a.ntiles;
+    const Q4<float>* __restrict__ Qin = a.Q[STAGE];
+    const Q4<float>* __restrict__ Qprev = a.Q[(STAGE + 2) % 3];
+    const Q4<float>* __restrict__ Gprev = a.G[(STAGE + 2) % 3];
+    Q4<float>* __restrict__ Gout = a.G[STAGE];
+
+    for (;;) {
+        if (tid == 0) {
+            int t = atomicAdd(a.counter + STAGE, 1);
+            if (t >= ntiles) {
+                t = -1;
+            } else {
+                td = a.tiles[t];
+                tp = a.P[td.sid];
+                const TileDesc& d = td;
+                const bool ok = d.ncore > 0 && d.ncore <= kTileCore && d.ncore + d.n1 <= kTileGrad &&
+                                d.ncore + d.n1 + d.n2 <= kTileCells && d.nr <= kTileRecs && d.ngeo <= kTileGeo &&
+                                d.nrc <= d.ngeo && d.ngeo <= d.nr && d.nrp >= d.nr && d.ngp >= d.ngeo &&
+                                5 * d.nrp + 3 * d.ngp <= kSmRecWords && d.ncsr <= kTileCsr && d.noff <= d.ncsr &&
+                                d.nhalo <= kTileCells && (d.nrp & 3) == 0 && (d.ngp & 3) == 0 && (d.ncsr & 7) == 0 &&
+                                (d.nhalo & 3) == 0 && (d.rec & 3) == 0 && (d.csr & 7) == 0 && (d.halo & 3) == 0;
+                if (!ok) {
+                    atomicOr(a.err, 4);
+                    t = -2;
+                } else {
+                    // the previous tile's generic accesses of this shared memory are complete
+                    // (barrier at the end of the loop); order them before the async-proxy writes
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    const uint32_t brec = 4u * (uint32_t)(5 * d.nrp + 3 * d.ngp), bcsr = 2u * (uint32_t)d.ncsr,
+                                   bhal = 4u * (uint32_t)d.nhalo, bq = 16u * (uint32_t)d.ncore;
+                    mbar_expect_tx(mb, brec + bcsr + bhal + bq);
+                    tma_load(srec, a.rec + d.rec, brec, mb);
+                    tma_load(scsr, a.csr + d.csr, bcsr, mb);
+                    if (bhal) tma_load(shalo, a.halo + d.halo, bhal, mb);
+                    tma_load(cq, Qin + d.c0, bq, mb);
+                }
+            }
+            s_tile = t;
+        }
+        __syncthreads();
+        const int t = s_tile;
+        if (t == -1) break;
+        if (t == -2) { __syncthreads(); continue; }
+        const bool ok = mbar_wait(mb, parity);
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) atomicOr(a.err, 2);
+            return;
+        }
+        parity ^= 1u;
+
+        const int ncore = td.ncore, n1 = td.n1, n2 = td.n2, nrp = td.nrp, ngp = td.ngp;
+        const int cbase = td.cbase, c0 = td.c0;
+        const Consts<float>& k = tp.k;
+        const bool order2 = tp.order2 != 0, ns = tp.ns != 0;
+        const bool fresh = STAGE == 0 && tp.fresh != 0, init_prims = STAGE == 0 && tp.init_prims != 0;
+        const bool squeeze = tp.squeeze != 0;
+        const uint32_t* __restrict__ r_sl = srec;
+        const float* __restrict__ r_d1x = reinterpret_cast<const float*>(srec + nrp);
+        const float* __restrict__ r_d1y = reinterpret_cast<const float*>(srec + 2 * nrp);
+        const float* __restrict__ r_d2x = reinterpret_cast<const float*>(srec + 3 * nrp);
+        const float* __restrict__ r_d2y = reinterpret_cast<const float*>(srec + 4 * nrp);
+        const float* __restrict__ r_nx = reinterpret_cast<const float*>(srec + 5 * nrp);
+        const float* __restrict__ r_ny = reinterpret_cast<const float*>(srec + 5 * nrp + ngp);
+        const float* __restrict__ r_A = reinterpret_cast<const float*>(srec + 5 * nrp + 2 * ngp);
+        const uint16_t* __restrict__ c_off = scsr;
+        const uint16_t* __restrict__ c_ent = scsr + td.noff;
+
+        // ---- gather: ring-1 (and, for gradients, ring-2) states
+        {
+            const int nh = order2 ? n1 + n2 : n1;
+            for (int i = tid; i < nh; i += blockDim.x) cq[ncore + i] = Qin[cbase + shalo[i]];
+        }
+        // the history flags act only on an iteration's first stage (STAGE 0); the second stage's
+        // kernel, which does not read them, clears them for the next iteration
+        if (STAGE == 1 && tid == 0) { a.P[td.sid].fresh = 0; a.P[td.sid].init_prims = 0; }
+        __syncthreads();
+
+        // ---- grad: limited LSQ gradients of the core and ring-1 cells
+        if (order2) {
+            for (int gI = tid; gI < ncore + n1; gI += blockDim.x) {
+                const int gid = gI < ncore ? c0 + gI : cbase + shalo[gI - ncore];
+                const float ixx = (float)a.Ixx[gid], iyy = (float)a.Iyy[gid], ixy = (float)a.Ixy[gid];
+                const bool lim_prev = squeeze && !fresh;
+                Q4<float> qp, gpx, gpy;
+                if (lim_prev) { qp = Qprev[gid]; gpx = Gprev[2 * (size_t)gid]; gpy = Gprev[2 * (size_t)gid + 1]; }
+                const Q4<float> qc = cq[gI];
+                float sx[4] = {0.f, 0.f, 0.f, 0.f}, sy[4] = {0.f, 0.f, 0.f, 0.f};
+                float qmin[4], qmax[4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) { qmin[j] = 100000000000.0f; qmax[j] = -100000000000.0f; }
+                const int e0 = c_off[gI], e1 = c_off[gI + 1];
+                for (int e = e0; e < e1; e++) {
+                    const int ent = c_ent[e], r = ent >> 1;
+                    const uint32_t sl = r_sl[r];
+                    const int s1 = (int)(sl & 0xFFFFu), s2 = (int)(int16_t)(sl >> 16);
+                    float d[4];
+                    if (s2 >= 0) {
+                        const Q4<float> q1 = cq[s1], q2 = cq[s2];
+#pragma unroll
+                        for (int j = 0; j < 4; j++) {
+                            d[j] = q2.p[j] - q1.p[j];
+                            if (squeeze) {
+                                qmin[j] = min2(qmin[j], min2(q1.p[j], q2.p[j]));
+                                qmax[j] = max2(qmax[j], max2(q1.p[j], q2.p[j]));
+                            }
+                        }
+                    } else {
+                        if (s2 == -1) {
+#pragma unroll
+                            for (int j = 0; j < 4; j++) d[j] = k.q_inf[j] - qc.p[j];
+                        } else if (s2 == -2 || s2 == -4) {
+                            float rho, u, v, P, yr;
+                            if (init_prims) { rho = k.rho_inf; u = k.u_inf; v = k.v_inf; P = k.P_inf; }
+                            else if (s2 == -2) tprims(qc.p, k, rho, u, v, P, yr);
+                            else {
+                                const Q4<float> qq = Qin[cbase + a.qcell[td.rbase + r]];
+                                tprims(qq.p, k, rho, u, v, P, yr);
+                            }
+                            float gq[4];
+                            if (s2 == -2) {   // slip wall: the cell velocity reflected (cell_gradient.cpp:43-55)
+                                const float fnx = r_nx[r], fny = r_ny[r];
+                                const float vn = u * fnx + v * fny;
+                                cons(rho, u - 2.0f * vn * fnx, v - 2.0f * vn * fny, P, k, gq);
+                            } else {          // no-slip: cell `face id`'s state, velocity negated (:62-73)
+                                cons(rho, -u, -v, P, k, gq);
+                            }
+#pragma unroll
+                            for (int j = 0; j < 4; j++) d[j] = gq[j] - qc.p[j];
+                        } else {
+#pragma unroll
+                            for (int j = 0; j < 4; j++) d[j] = 0.f;
+                        }
+                        if (squeeze)
+#pragma unroll
+                            for (int j = 0; j < 4; j++) { qmin[j] = min2(qmin[j], qc.p[j]); qmax[j] = max2(qmax[j], qc.p[j]); }
+                    }
+                    const float fx = r_d1x[r] - r_d2x[r], fy = r_d1y[r] - r_d2y[r];
+#pragma unroll
+                    for (int j = 0; j < 4; j++) { sx[j] += d[j] * fx; sy[j] += d[j] * fy; }
+                }
+                Q4<float> gx, gy;
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    gx.p[j] = sx[j] * iyy - sy[j] * ixy;
+                    gy.p[j] = sy[j] * ixx - sx[j] * ixy;
+                }
+                if (squeeze) {
+                    // the previous stage's face values on this cell's side (res.cpp:40 runs before :48)
+                    float phi[4] = {1.f, 1.f, 1.f, 1.f};
+                    for (int e = e0; e < e1; e++) {
+                        const int ent = c_ent[e], r = ent >> 1, side = ent & 1;
+                        const float dx = side ? r_d2x[r] : r_d1x[r], dy = side ? r_d2y[r] : r_d1y[r];
+#pragma unroll
+                        for (int j = 0; j < 4; j++) {
+                            const float qf = lim_prev ? qp.p[j] + gpx.p[j] * dx + gpy.p[j] * dy : -101.0f;
+                            float ph = 1.0f;
+                            if (less(qf, qmin[j])) ph = (qmin[j] - qc.p[j]) / (qf - qc.p[j]);
+                            else if (less(qmax[j], qf)) ph = (qmax[j] - qc.p[j]) / (qf - qc.p[j]);
+                            phi[j] = min2(ph, phi[j]);
+                        }
+                    }
+#pragma unroll
+                    for (int j = 0; j < 4; j++) { gx.p[j] *= phi[j]; gy.p[j] *= phi[j]; }
+                }
+                cg[2 * gI] = gx;
+                cg[2 * gI + 1] = gy;
+                if (gI < ncore) { Gout[2 * (size_t)gid] = gx; Gout[2 * (size_t)gid + 1] = gy; }
+            }
+            __syncthreads();
+        }
+
+        // ---- flux: every face of a core cell; V*A - F*A (and the spectral term) replace its geometry
+        {
+            float* w_t0 = reinterpret_cast<float*>(srec + nrp);
+            float* w_t1 = reinterpret_cast<float*>(srec + 2 * nrp);
+            float* w_t2 = reinterpret_cast<float*>(srec + 3 * nrp);
+            float* w_t3 = reinterpret_cast<float*>(srec + 4 * nrp);
+            float* w_sp = reinterpret_cast<float*>(srec + 5 * nrp);
+            for (int r = tid; r < td.nrc; r += blockDim.x) {
+                const uint32_t sl = r_sl[r];
+                const int s1 = (int)(sl & 0xFFFFu), s2 = (int)(int16_t)(sl >> 16);
+                const float d1x = r_d1x[r], d1y = r_d1y[r], d2x = r_d2x[r], d2y = r_d2y[r];
+                const float fnx = r_nx[r], fny = r_ny[r], A = r_A[r];
+                const Q4<float> q1 = cq[s1];
+                Q4<float> g1x, g1y;
+                if (order2) { g1x = cg[2 * s1]; g1y = cg[2 * s1 + 1]; }
+                else {
+#pragma unroll
+                    for (int j = 0; j < 4; j++) { g1x.p[j] = 0.f; g1y.p[j] = 0.f; }
+                }
+                float L[4], Rq[4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) L[j] = q1.p[j] + g1x.p[j] * d1x + g1y.p[j] * d1y;
+                float lrho, lu, lv, lP, ly;
+                tprims(L, k, lrho, lu, lv, lP, ly);
+                const float lc = sqrtf(k.gamma * lP * ly);
+                Q4<float> q2, g2x, g2y;
+                if (s2 >= 0) {
+                    q2 = cq[s2];
+                    if (order2) { g2x = cg[2 * s2]; g2y = cg[2 * s2 + 1]; }
+                    else {
+#pragma unroll
+                        for (int j = 0; j < 4; j++) { g2x.p[j] = 0.f; g2y.p[j] = 0.f; }
+                    }
+#pragma unroll
+                    for (int j = 0; j < 4; j++) Rq[j] = q2.p[j] + g2x.p[j] * d2x + g2y.p[j] * d2y;
+                } else if (s2 == -1) {
+#pragma unroll
+                    for (int j = 0; j < 4; j++) Rq[j] = k.q_inf[j];
+                } else if (s2 == -2) {
+                    const float vn = lu * fnx + lv * fny;
+                    cons(lrho, lu - 2.0f * vn * fnx, lv - 2.0f * vn * fny, lP, k, Rq);
+                } else if (s2 == -3) {
+#pragma unroll
+                    for (int j = 0; j < 4; j++) Rq[j] = L[j];
+                } else {
+                    cons(lrho, -lu, -lv, lP, k, Rq);
+                }
+                float rrho, ru, rv, rP, ry;
+                tprims(Rq, k, rrho, ru, rv, rP, ry);
+                const float rc = sqrtf(k.gamma * rP * ry);
+                const float vn1 = lu * fnx + lv * fny, vn2 = ru * fnx + rv * fny;
+                const float vna = 0.5f * (vn1 + vn2), ca = 0.5f * (lc + rc);
+                const float lam = 0.5f * (fabsf(vna) + ca);
+                float Fr[4];
+                {
+                    const float F1[4] = {lrho * vn1, lrho * lu * vn1 + lP * fnx, lrho * lv * vn1 + lP * fny, vn1 * (L[3] + lP)};
+                    const float F2[4] = {rrho * vn2, rrho * ru * vn2 + rP * fnx, rrho * rv * vn2 + rP * fny, vn2 * (Rq[3] + rP)};
+#pragma unroll
+                    for (int j = 0; j < 4; j++) Fr[j] = k.roe ? -101.0f : 0.5f * (F1[j] + F2[j]) - lam * (Rq[j] - L[j]);
+                }
+                float V[4] = {0.f, 0.f, 0.f, 0.f};
+                if (ns && order2) {   // first order never adds the viscous flux (res.cpp:27-29,50-53)
+                    float Aq[4];
+#pragma unroll
+                    for (int j = 0; j < 4; j++) Aq[j] = 0.5f * (L[j] + Rq[j]);
+                    float arho, au, av, aP, ya;
+                    tprims(Aq, k, arho, au, av, aP, ya);
+                    float ux = 0.f, uy = 0.f, vx = 0.f, vy = 0.f, Px = 0.f, Py = 0.f, rx = 0.f, rly = 0.f;
+                    bool have = true;
+                    if (s2 >= 0) {
+                        // l: unit vector c1 -> c2 (the LSQ displacement d1 - d2), m = (-ny, nx)
+                        const float tx = d1x - d2x, ty = d1y - d2y;
+                        const float yd = rsqrtf(tx * tx + ty * ty);
+                        const float lxf = tx * yd, lyf = ty * yd, mxf = -fny, myf = fnx;
+                        float dQx[4], dQy[4];
+#pragma unroll
+                        for (int j = 0; j < 4; j++) {
+                            const float dl = (q2.p[j] - q1.p[j]) * yd;
+                            const float dm = 0.5f * (g1x.p[j] * mxf + g1y.p[j] * myf + g2x.p[j] * mxf + g2y.p[j] * myf);
+                            dQy[j] = (dl + dm) * lyf;   // reconstruction.cpp:138-146: l for both terms
+                            dQx[j] = (dl + dm) * lxf;
+                        }
+                        rx = dQx[0];
+                        ux = dQx[1] - rx * au * ya;
+                        vx = dQx[2] - rx * av * ya;
+                        rly = dQy[0];
+                        uy = dQy[1] - rly * au * ya;
+                        vy = dQy[2] - rly * au * ya;   // reconstruction.cpp:155 uses u
+                        Px = k.gm1 * (dQx[3] - 0.5f * rx * (au * au + av * av) - arho * (au * ux + av * vx));
+                        Py = k.gm1 * (dQy[3] - 0.5f * rly * (au * au + av * av) - arho * (au * uy + av * vy));
+                    } else if (s2 == -4) {
+                        const float ydn = rsqrtf(d1x * d1x + d1y * d1y);
+                        float cu, cv;
+                        if (init_prims) { cu = k.u_inf; cv = k.v_inf; }
+                        else { const float yq = 1.0f / q1.p[0]; cu = q1.p[1] * yq; cv = q1.p[2] * yq; }
+                        const float dudn = -cu * ydn, dvdn = -cv * ydn;
+                        ux = dudn * fnx; uy = dudn * fny;
+                        vx = dvdn * fnx; vy = dvdn * fny;
+                    } else if (s2 == -2) {
+                        have = false;   // SLIP_WALL with NS: tau and grad T stay zero (:104-106)
+                    }
+                    if (have) {
+                        const float third = (ux + vy) * (1.0f / 3.0f);
+                        const float txx = 2.0f * k.mu * (ux - third), txy = k.mu * (uy + vx), tyy = 2.0f * k.mu * (vy - third);
+                        const float yden = 1.0f / (k.R * arho * arho);
+                        const float dTx = (Px * arho - rx * aP) * yden, dTy = (Py * arho - rly * aP) * yden;
+                        V[1] = txx * fnx + txy * fny;
+                        V[2] = txy * fnx + tyy * fny;
+                        V[3] = fnx * (au * txx + av * txy + k.k * dTx) + fny * (au * txy + av * tyy + k.k * dTy);
+                    }
+                }
+                w_t0[r] = (V[0] - Fr[0]) * A;
+                w_t1[r] = (V[1] - Fr[1]) * A;
+                w_t2[r] = (V[2] - Fr[2]) * A;
+                w_t3[r] = (V[3] - Fr[3]) * A;
+                if (STAGE == 2) w_sp[r] = k.roe ? (fabsf(k.vn0) + k.c0) * A : (fabsf(vna) + ca) * A;
+            }
+        }
+        __syncthreads();
+
+        // ---- update: residual gather, time step, SSP-RK3 stage of the core cells
+        float snext = 0.f;
+        double r2[4] = {0.0, 0.0, 0.0, 0.0};
+        if (tid < ncore) {
+            const int c = tid, gid = c0 + c;
+            const float* t0 = reinterpret_cast<const float*>(srec + nrp);
+            const float* t1 = reinterpret_cast<const float*>(srec + 2 * nrp);
+            const float* t2 = reinterpret_cast<const float*>(srec + 3 * nrp);
+            const float* t3 = reinterpret_cast<const float*>(srec + 4 * nrp);
+            const float* sp = reinterpret_cast<const float*>(srec + 5 * nrp);
+            // the stage's cell data, requested before the gather
+            const float yv = a.rvol[gid];
+            float dtc = 0.f, sc = 0.f, vc = 0.f;
+            if (STAGE == 0) { vc = a.vol[gid]; if (!tp.global_dt) sc = a.S[gid]; }
+            else dtc = a.dt[gid];
+            Q4<float> qn, dprev, lo;
+            if (STAGE == 0) qn = cq[c];
+            else { qn = a.Q[0][gid]; dprev = a.D[gid]; }
+            if (STAGE == 2) lo = a.Qlo[gid];
+            float r4[4] = {0.f, 0.f, 0.f, 0.f};
+            const int e0 = c_off[c], e1 = c_off[c + 1];
+            for (int e = e0; e < e1; e++) {
+                const int ent = c_ent[e], r = ent >> 1, side = ent & 1;
+                r4[0] += neg_if(t0[r], side);
+                r4[1] += neg_if(t1[r], side);
+                r4[2] += neg_if(t2[r], side);
+                r4[3] += neg_if(t3[r], side);
+                if (STAGE == 2) snext += sp[r];
+            }
+#pragma unroll
+            for (int j = 0; j < 4; j++) r4[j] *= yv;
+            if (a.R && (a.store_r || STAGE == 2)) { Q4<float> rr; for (int j = 0; j < 4; j++) rr.p[j] = r4[j]; a.R[gid] = rr; }
+            if (STAGE == 0) {
+                dtc = (k.two_cfl * vc) / (tp.global_dt ? a.smax[td.sid] : sc);
+                a.dt[gid] = dtc;
+            }
+            Q4<float> out, dn;
+            if (STAGE == 0) {
+#pragma unroll
+                for (int j = 0; j < 4; j++) { dn.p[j] = dtc * r4[j]; out.p[j] = qn.p[j] + dn.p[j]; }
+                a.D[gid] = dn;
+                a.Q[1][gid] = out;
+            } else if (STAGE == 1) {
+#pragma unroll
+                for (int j = 0; j < 4; j++) { dn.p[j] = 0.25f * dprev.p[j] + 0.25f * dtc * r4[j]; out.p[j] = qn.p[j] + dn.p[j]; }
+                a.D[gid] = dn;
+                a.Q[2][gid] = out;
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const float inc = (2.0f / 3.0f) * dprev.p[j] + (2.0f / 3.0f) * dtc * r4[j];
+                    float s, err;
+                    two_sum(qn.p[j], lo.p[j] + inc, s, err);
+                    out.p[j] = s;
+                    lo.p[j] = err;
+                }
+                a.Q[0][gid] = out;
+                a.Qlo[gid] = lo;
+                a.S[gid] = snext;
+#pragma unroll
+                for (int j = 0; j < 4; j++) r2[j] = (double)r4[j] * (double)r4[j];
+            }
+            if (!positive(out.p[0]) || !positive(out.p[3])) atomicOr(a.flags + td.sid, 1);
+        }
+        if (STAGE == 2) {
+            // per tile: the spectral maximum (GLOBAL dt of the next iteration) and the residual sums
+            // of squares (the batch's per-solve norms), each reduced in a fixed order
+            float m = snext;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) m = max2(m, __shfl_xor_sync(0xffffffffu, m, o));
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) r2[j] += __shfl_xor_sync(0xffffffffu, r2[j], o);
+            if (lane == 0) {
+                redf[warp] = m;
+#pragma unroll
+                for (int j = 0; j < 4; j++) redd[j][warp] = r2[j];
+            }
+            __syncthreads();
+            if (tid == 0) {
+                float bm = 0.f;
+                double bs[4] = {0.0, 0.0, 0.0, 0.0};
+                for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+                    bm = max2(bm, redf[w]);
+                    for (int j = 0; j < 4; j++) bs[j] += redd[j][w];
+                }
+                atomic_max_pos(a.smax + td.sid, bm);
+                if (a.tpart)
+                    for (int j = 0; j < 4; j++) a.tpart[4 * (size_t)t + j] = bs[j];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Initial spectral sums of a solve's tiles (the initial Vn_avg, c_avg of every face,
+// class_q.hpp:61-62) in each cell's csr order, and their maximum.
+__global__ void __launch_bounds__(kTileCore) k_tspec_init(const TileDesc* __restrict__ tiles, int first, int count,
+                                                        const uint32_t* __restrict__ rec, const uint16_t* __restrict__ csr,
+                                                        const TParams* __restrict__ P, float* __restrict__ S,
+                                                        float* __restrict__ smax) {
+    __shared__ float red[kTileCore / 32];
+    for (int t = first + blockIdx.x; t < first + count; t += gridDim.x) {
+        const TileDesc d = tiles[t];
+        const Consts<float>& k = P[d.sid].k;
+        float s = 0.f;
+        if ((int)threadIdx.x < d.ncore) {
+            const uint16_t* off = csr + d.csr;
+            const uint16_t* ent = off + d.noff;
+            const float* A = reinterpret_cast<const float*>(rec + d.rec + 5 * (size_t)d.nrp + 2 * (size_t)d.ngp);
+            for (int e = off[threadIdx.x]; e < off[threadIdx.x + 1]; e++) s += (fabsf(k.vn0) + k.c0) * A[ent[e] >> 1];
+            S[d.c0 + threadIdx.x] = s;
+        }
+        float m = s;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = max2(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float bm = 0.f;
+            for (int w = 0; w < (int)(blockDim.x >> 5); w++) bm = max2(bm, red[w]);
+            atomic_max_pos(smax + d.sid, bm);
+        }
+        __syncthreads();
+    }
+}
+
+// Per-solve residual sums of squares: solve s owns tiles [srange[2s], srange[2s] + srange[2s+1]);
+// one block per solve slot adds their per-tile sums in a fixed order.
+__global__ void __launch_bounds__(256) k_tres_norm(const int* __restrict__ srange, const double* __restrict__ tpart,
+                                                   double* __restrict__ res2) {
+    __shared__ double sh[4][256];
+    const int s = blockIdx.x, first = srange[2 * s], n = srange[2 * s + 1];
+    double acc[4] = {0, 0, 0, 0};
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[j] += tpart[4 * (size_t)(first + i) + j];
+#pragma unroll
+    for (int j = 0; j < 4; j++) sh[j][threadIdx.x] = acc[j];
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h)
+#pragma unroll
+            for (int j = 0; j < 4; j++) sh[j][threadIdx.x] += sh[j][threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int j = 0; j < 4; j++) res2[4 * s + j] = sh[j][0];
+}
+
+}  // namespace fv2d

@@ -455,6 +455,8 @@ class Batch:
         return int(b.value), tuple(int(x) for x in tm), tuple(int(x) for x in be)
 
     def usage(self):
+        """Arena use.  FP64: cells, faces, incidences; FP32 (tile layout): cells, face records and
+        csr words, reported under the same keys."""
         o = (ctypes.c_longlong * 8)()
         _check(library().fv2d_batch_usage(self.h, o))
         keys = ("cells_used", "cells_cap", "faces_used", "faces_cap", "incs_used", "incs_cap", "active", "bytes")
@@ -467,7 +469,9 @@ class Batch:
         ms = np.zeros(3, np.float64)
         ln = np.zeros(3, np.int32)
         _check(library().fv2d_batch_kernel_times(self.h, _dp(ms), _ip(ln)))
-        return {k: (float(ms[i]), int(ln[i])) for i, k in enumerate(("kb_gradient", "kb_face", "kb_update"))}
+        names = (("kb_gradient", "kb_face", "kb_update") if self.precision == FP64
+                 else ("k_tstage_1", "k_tstage_2", "k_tstage_3"))   # FP32: the fused kernel of each RK stage
+        return {k: (float(ms[i]), int(ln[i])) for i, k in enumerate(names)}
 
     def stream(self) -> int:
         return int(library().fv2d_batch_stream(self.h) or 0)

@@ -129,7 +129,7 @@ def test_batch_admission(pkg):
         b.add(g, c)                # no room left: refused, batch unchanged
     assert e.value.code == 6
     u = b.usage()
-    assert u["active"] == 1 and u["cells_used"] == g.num_cells + 1
+    assert u["active"] == 1 and g.num_cells <= u["cells_used"] <= g.num_cells + 4
     b.step(2)
     assert len(b.norms()) == 1
     b.close()
