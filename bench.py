@@ -370,7 +370,9 @@ def measure_fp32(pkg, grid, case, args, peak, peak_kind, N, F, ninc, Nb):
     s.step(args.steps)
     kt = s.kernel_times()
     s.close()
-    dom, roof, per = roofline(kt, single_kernel_bytes(N, F, ninc, Nb, 4, True), peak)
+    # the FP32 engine runs one fused kernel per stage: its algorithmic bytes are the whole stage's
+    ns = case["eqn"] == "NS"
+    dom, roof, per = roofline(kt, {"k_tstage": bytes_8d(N, F, Nb, 4, ns, case["limiter"] == "SQUEEZE")}, peak)
     roof["peak_source"] = f"{peak_kind} hbm_gbs"
     roof["traffic"] = ncu_traffic("fp32", dom, N, F)
     add_step_8d(roof, [(N, F, Nb, 4, case["eqn"] == "NS", case["limiter"] == "SQUEEZE")], ms / args.steps, peak)
@@ -413,12 +415,10 @@ def measure_batched(pkg, args, peak, peak_kind):
     b.step(max(3, args.steps // 4))
     kt = b.kernel_times()
     b.set_kernel_timing(False)
-    kbytes = {"kb_gradient": 0.0, "kb_face": 0.0, "kb_update": 0.0}
-    for g, sp in zip(grids, specs):
-        nb = int((g.fc2 <= 0).sum())
-        for k in kbytes:
-            kbytes[k] += bytes_per_launch(k, g.num_cells, g.num_faces, 2 * g.num_faces - nb, nb, 4, sp["ns"], True,
-                                          comp=True, store_r=False)
+    # one fused kernel per stage (k_tstage_1..3), each moving a whole stage's algorithmic bytes
+    stage_bytes = sum(bytes_8d(g.num_cells, g.num_faces, int((g.fc2 <= 0).sum()), 4, bool(sp["ns"]), True)
+                      for g, sp in zip(grids, specs))
+    kbytes = {k: stage_bytes for k in ("k_tstage_1", "k_tstage_2", "k_tstage_3")}
     dom, roof, per = roofline(kt, kbytes, peak)
     roof["peak_source"] = f"{peak_kind} hbm_gbs"
     roof["traffic"] = ncu_traffic("batch_fp32", dom, tot_c, tot_f)

@@ -13,6 +13,7 @@
 #include "fv2d_output.h"
 #include "fv2d_batch.h"
 #include "fv2d_solver.h"
+#include "fv2d_tiles.h"
 
 namespace {
 // Named NVTX range around a C-ABI call (shows the library's calls on an Nsight timeline).
@@ -159,6 +160,20 @@ int fv2d_mesh_permutation(const fv2d_mesh* mm, int kind, int* out) {
     if (!mm || !out) return fail(FV2D_ERR_ARG, "null argument");
     const std::vector<int>& p = kind == 0 ? mm->m.cell_new2old : mm->m.face_new2old;
     std::copy(p.begin(), p.end(), out);
+    return FV2D_OK;
+}
+
+int fv2d_mesh_tiles(const fv2d_mesh* mm, long long* o) {
+    if (!mm || !o) return fail(FV2D_ERR_ARG, "null argument");
+    fv2d::DeviceLayout L;
+    fv2d::build_layout(mm->m, L);
+    fv2d::TileLayout T;
+    std::string err;
+    if (!fv2d::build_tile_layout(mm->m, L, T, err)) return fail(FV2D_ERR_MESH, err);
+    long long nrc = 0, r1 = 0, r2 = 0;
+    for (const auto& t : T.tiles) { nrc += t.nrc; r1 += t.n1; r2 += t.n2; }
+    o[0] = (long long)T.tiles.size(); o[1] = (long long)T.rec.size(); o[2] = (long long)T.qcell.size();
+    o[3] = (long long)T.csr.size(); o[4] = (long long)T.halo.size(); o[5] = nrc; o[6] = r1; o[7] = r2;
     return FV2D_OK;
 }
 

@@ -524,9 +524,15 @@ public:
         rc = core_.prepare();
         if (rc) { err_ = core_.err; return rc; }
         n2o_ = im->n2o;
-        FV2D_T(cudaMalloc(&dstage_, 8 * 8 * (size_t)nc_ + 4 * (size_t)nc_ + 32 * 304));
-        dn2o_ = (int*)((char*)dstage_ + 8 * 8 * (size_t)nc_);
-        part_ = (double*)((char*)dn2o_ + 4 * (size_t)nc_);
+        // one allocation: field staging (8 doubles per cell), the cell permutation and the norm
+        // partials, each region starting on a 256-byte boundary
+        size_t off = 0;
+        auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) & ~size_t(255); return o; };
+        take(8 * 8 * (size_t)nc_);
+        const size_t o_n2o = take(4 * (size_t)nc_), o_part = take(32 * 304);
+        FV2D_T(cudaMalloc(&dstage_, off));
+        dn2o_ = (int*)((char*)dstage_ + o_n2o);
+        part_ = (double*)((char*)dstage_ + o_part);
         staging_bytes_ = std::max<size_t>(8 * 8 * (size_t)nc_, 32 * 304);
         FV2D_T(cudaMallocHost(&host_stage_, staging_bytes_));
         FV2D_T(cudaEventCreateWithFlags(&stage_free_, cudaEventDisableTiming));

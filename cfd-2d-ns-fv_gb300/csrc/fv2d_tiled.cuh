@@ -209,65 +209,76 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
         if (order2) {
             for (int gI = tid; gI < ncore + n1; gI += blockDim.x) {
                 const int gid = gI < ncore ? c0 + gI : cbase + shalo[gI - ncore];
-                const float ixx = (float)a.Ixx[gid], iyy = (float)a.Iyy[gid], ixy = (float)a.Ixy[gid];
                 const bool lim_prev = squeeze && !fresh;
+                // requested first: used only after the loop over the cell's faces
+                const double dxx = a.Ixx[gid], dyy = a.Iyy[gid], dxy = a.Ixy[gid];
                 Q4<float> qp, gpx, gpy;
                 if (lim_prev) { qp = Qprev[gid]; gpx = Gprev[2 * (size_t)gid]; gpy = Gprev[2 * (size_t)gid + 1]; }
                 const Q4<float> qc = cq[gI];
+                // LSQ sums (Q(c2) - Q(c1)) * (dxj, dyj) over the cell's faces, the bounds of the cell and
+                // its neighbours, and - for the squeeze limiter - the extremes over the faces of
+                // t = (previous stage's face value on this cell's side) - (this cell's value)
                 float sx[4] = {0.f, 0.f, 0.f, 0.f}, sy[4] = {0.f, 0.f, 0.f, 0.f};
-                float qmin[4], qmax[4];
+                float qmin[4], qmax[4], tmin[4], tmax[4], base[4];
 #pragma unroll
-                for (int j = 0; j < 4; j++) { qmin[j] = 100000000000.0f; qmax[j] = -100000000000.0f; }
+                for (int j = 0; j < 4; j++) {
+                    qmin[j] = qc.p[j]; qmax[j] = qc.p[j];
+                    tmin[j] = 3.0e38f; tmax[j] = -3.0e38f;
+                    base[j] = lim_prev ? qp.p[j] - qc.p[j] : -101.0f - qc.p[j];   // -101: fresh face history
+                }
                 const int e0 = c_off[gI], e1 = c_off[gI + 1];
                 for (int e = e0; e < e1; e++) {
-                    const int ent = c_ent[e], r = ent >> 1;
+                    const int ent = c_ent[e], r = ent >> 1, side = ent & 1;
                     const uint32_t sl = r_sl[r];
                     const int s1 = (int)(sl & 0xFFFFu), s2 = (int)(int16_t)(sl >> 16);
+                    const int so = side ? s1 : s2;          // the face's other cell (or BC code)
+                    const float d1x = r_d1x[r], d1y = r_d1y[r], d2x = r_d2x[r], d2y = r_d2y[r];
                     float d[4];
-                    if (s2 >= 0) {
-                        const Q4<float> q1 = cq[s1], q2 = cq[s2];
+                    if (so >= 0) {
+                        const Q4<float> qn = cq[so];
 #pragma unroll
                         for (int j = 0; j < 4; j++) {
-                            d[j] = q2.p[j] - q1.p[j];
-                            if (squeeze) {
-                                qmin[j] = min2(qmin[j], min2(q1.p[j], q2.p[j]));
-                                qmax[j] = max2(qmax[j], max2(q1.p[j], q2.p[j]));
-                            }
+                            d[j] = side ? qc.p[j] - qn.p[j] : qn.p[j] - qc.p[j];   // reference orientation c2 - c1
+                            qmin[j] = fminf(qmin[j], qn.p[j]);
+                            qmax[j] = fmaxf(qmax[j], qn.p[j]);
                         }
+                    } else if (so == -1) {
+#pragma unroll
+                        for (int j = 0; j < 4; j++) d[j] = k.q_inf[j] - qc.p[j];
+                    } else if (so == -2 || so == -4) {
+                        float rho, u, v, P, yr;
+                        if (init_prims) { rho = k.rho_inf; u = k.u_inf; v = k.v_inf; P = k.P_inf; }
+                        else if (so == -2) tprims(qc.p, k, rho, u, v, P, yr);
+                        else {
+                            const Q4<float> qq = Qin[cbase + a.qcell[td.rbase + r]];
+                            tprims(qq.p, k, rho, u, v, P, yr);
+                        }
+                        float gq[4];
+                        if (so == -2) {   // slip wall: the cell velocity reflected (cell_gradient.cpp:43-55)
+                            const float fnx = r_nx[r], fny = r_ny[r];
+                            const float vn = u * fnx + v * fny;
+                            cons(rho, u - 2.0f * vn * fnx, v - 2.0f * vn * fny, P, k, gq);
+                        } else {          // no-slip: cell `face id`'s state, velocity negated (:62-73)
+                            cons(rho, -u, -v, P, k, gq);
+                        }
+#pragma unroll
+                        for (int j = 0; j < 4; j++) d[j] = gq[j] - qc.p[j];
                     } else {
-                        if (s2 == -1) {
 #pragma unroll
-                            for (int j = 0; j < 4; j++) d[j] = k.q_inf[j] - qc.p[j];
-                        } else if (s2 == -2 || s2 == -4) {
-                            float rho, u, v, P, yr;
-                            if (init_prims) { rho = k.rho_inf; u = k.u_inf; v = k.v_inf; P = k.P_inf; }
-                            else if (s2 == -2) tprims(qc.p, k, rho, u, v, P, yr);
-                            else {
-                                const Q4<float> qq = Qin[cbase + a.qcell[td.rbase + r]];
-                                tprims(qq.p, k, rho, u, v, P, yr);
-                            }
-                            float gq[4];
-                            if (s2 == -2) {   // slip wall: the cell velocity reflected (cell_gradient.cpp:43-55)
-                                const float fnx = r_nx[r], fny = r_ny[r];
-                                const float vn = u * fnx + v * fny;
-                                cons(rho, u - 2.0f * vn * fnx, v - 2.0f * vn * fny, P, k, gq);
-                            } else {          // no-slip: cell `face id`'s state, velocity negated (:62-73)
-                                cons(rho, -u, -v, P, k, gq);
-                            }
-#pragma unroll
-                            for (int j = 0; j < 4; j++) d[j] = gq[j] - qc.p[j];
-                        } else {
-#pragma unroll
-                            for (int j = 0; j < 4; j++) d[j] = 0.f;
-                        }
-                        if (squeeze)
-#pragma unroll
-                            for (int j = 0; j < 4; j++) { qmin[j] = min2(qmin[j], qc.p[j]); qmax[j] = max2(qmax[j], qc.p[j]); }
+                        for (int j = 0; j < 4; j++) d[j] = 0.f;
                     }
-                    const float fx = r_d1x[r] - r_d2x[r], fy = r_d1y[r] - r_d2y[r];
+                    const float fx = d1x - d2x, fy = d1y - d2y;   // LSQ displacement c1 -> c2 (or ghost)
+                    const float ox = side ? d2x : d1x, oy = side ? d2y : d1y;   // face centre - this cell
 #pragma unroll
-                    for (int j = 0; j < 4; j++) { sx[j] += d[j] * fx; sy[j] += d[j] * fy; }
+                    for (int j = 0; j < 4; j++) {
+                        sx[j] += d[j] * fx;
+                        sy[j] += d[j] * fy;
+                        const float t = lim_prev ? base[j] + gpx.p[j] * ox + gpy.p[j] * oy : base[j];
+                        tmin[j] = fminf(tmin[j], t);
+                        tmax[j] = fmaxf(tmax[j], t);
+                    }
                 }
+                const float ixx = (float)dxx, iyy = (float)dyy, ixy = (float)dxy;
                 Q4<float> gx, gy;
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
@@ -275,22 +286,18 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
                     gy.p[j] = sy[j] * ixx - sx[j] * ixy;
                 }
                 if (squeeze) {
-                    // the previous stage's face values on this cell's side (res.cpp:40 runs before :48)
-                    float phi[4] = {1.f, 1.f, 1.f, 1.f};
-                    for (int e = e0; e < e1; e++) {
-                        const int ent = c_ent[e], r = ent >> 1, side = ent & 1;
-                        const float dx = side ? r_d2x[r] : r_d1x[r], dy = side ? r_d2y[r] : r_d1y[r];
+                    // squeeze (squeeze.cpp:68-141): phi = the smallest (bound - Q) / (face value - Q) over
+                    // the faces whose previous face value leaves [Qmin, Qmax]; as x -> (bound - Q) / x is
+                    // monotone on either side of zero, that is the quotient at the extreme t
 #pragma unroll
-                        for (int j = 0; j < 4; j++) {
-                            const float qf = lim_prev ? qp.p[j] + gpx.p[j] * dx + gpy.p[j] * dy : -101.0f;
-                            float ph = 1.0f;
-                            if (less(qf, qmin[j])) ph = (qmin[j] - qc.p[j]) / (qf - qc.p[j]);
-                            else if (less(qmax[j], qf)) ph = (qmax[j] - qc.p[j]) / (qf - qc.p[j]);
-                            phi[j] = min2(ph, phi[j]);
-                        }
+                    for (int j = 0; j < 4; j++) {
+                        const float up = qmax[j] - qc.p[j], dn = qmin[j] - qc.p[j];
+                        float phi = 1.0f;
+                        if (tmax[j] > up) phi = fminf(phi, up / tmax[j]);
+                        if (tmin[j] < dn) phi = fminf(phi, dn / tmin[j]);
+                        gx.p[j] *= phi;
+                        gy.p[j] *= phi;
                     }
-#pragma unroll
-                    for (int j = 0; j < 4; j++) { gx.p[j] *= phi[j]; gy.p[j] *= phi[j]; }
                 }
                 cg[2 * gI] = gx;
                 cg[2 * gI + 1] = gy;
@@ -306,34 +313,52 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
             float* w_t2 = reinterpret_cast<float*>(srec + 3 * nrp);
             float* w_t3 = reinterpret_cast<float*>(srec + 4 * nrp);
             float* w_sp = reinterpret_cast<float*>(srec + 5 * nrp);
+            const bool visc = ns && order2;   // first order never adds the viscous flux (res.cpp:27-29,50-53)
             for (int r = tid; r < td.nrc; r += blockDim.x) {
                 const uint32_t sl = r_sl[r];
                 const int s1 = (int)(sl & 0xFFFFu), s2 = (int)(int16_t)(sl >> 16);
                 const float d1x = r_d1x[r], d1y = r_d1y[r], d2x = r_d2x[r], d2y = r_d2y[r];
-                const float fnx = r_nx[r], fny = r_ny[r], A = r_A[r];
-                const Q4<float> q1 = cq[s1];
-                Q4<float> g1x, g1y;
-                if (order2) { g1x = cg[2 * s1]; g1y = cg[2 * s1 + 1]; }
-                else {
+                const float fnx = r_nx[r], fny = r_ny[r];
+                const float mxf = -fny, myf = fnx;   // unit tangent p1 -> p2
+                // face states; for NS also the face-average tangential derivative m.(grad Q1 + grad Q2)/2,
+                // the difference Q2 - Q1 and c1's velocity, so the cell states and gradients die early
+                float L[4], Rq[4], dm[4], dq[4];
+                float cu = 0.f, cv = 0.f;
+                {
+                    const Q4<float> q1 = cq[s1];
+                    Q4<float> g1x, g1y;
+                    if (order2) { g1x = cg[2 * s1]; g1y = cg[2 * s1 + 1]; }
+                    else {
 #pragma unroll
-                    for (int j = 0; j < 4; j++) { g1x.p[j] = 0.f; g1y.p[j] = 0.f; }
+                        for (int j = 0; j < 4; j++) { g1x.p[j] = 0.f; g1y.p[j] = 0.f; }
+                    }
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        L[j] = q1.p[j] + g1x.p[j] * d1x + g1y.p[j] * d1y;
+                        dm[j] = g1x.p[j] * mxf + g1y.p[j] * myf;
+                        dq[j] = -q1.p[j];
+                    }
+                    if (visc && s2 == -4) {
+                        if (init_prims) { cu = k.u_inf; cv = k.v_inf; }
+                        else { const float yq = 1.0f / q1.p[0]; cu = q1.p[1] * yq; cv = q1.p[2] * yq; }
+                    }
                 }
-                float L[4], Rq[4];
-#pragma unroll
-                for (int j = 0; j < 4; j++) L[j] = q1.p[j] + g1x.p[j] * d1x + g1y.p[j] * d1y;
                 float lrho, lu, lv, lP, ly;
                 tprims(L, k, lrho, lu, lv, lP, ly);
-                const float lc = sqrtf(k.gamma * lP * ly);
-                Q4<float> q2, g2x, g2y;
                 if (s2 >= 0) {
-                    q2 = cq[s2];
+                    const Q4<float> q2 = cq[s2];
+                    Q4<float> g2x, g2y;
                     if (order2) { g2x = cg[2 * s2]; g2y = cg[2 * s2 + 1]; }
                     else {
 #pragma unroll
                         for (int j = 0; j < 4; j++) { g2x.p[j] = 0.f; g2y.p[j] = 0.f; }
                     }
 #pragma unroll
-                    for (int j = 0; j < 4; j++) Rq[j] = q2.p[j] + g2x.p[j] * d2x + g2y.p[j] * d2y;
+                    for (int j = 0; j < 4; j++) {
+                        Rq[j] = q2.p[j] + g2x.p[j] * d2x + g2y.p[j] * d2y;
+                        dm[j] = 0.5f * (dm[j] + g2x.p[j] * mxf + g2y.p[j] * myf);
+                        dq[j] += q2.p[j];
+                    }
                 } else if (s2 == -1) {
 #pragma unroll
                     for (int j = 0; j < 4; j++) Rq[j] = k.q_inf[j];
@@ -346,6 +371,8 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
                 } else {
                     cons(lrho, -lu, -lv, lP, k, Rq);
                 }
+                const float A = r_A[r];
+                const float lc = sqrtf(k.gamma * lP * ly);
                 float rrho, ru, rv, rP, ry;
                 tprims(Rq, k, rrho, ru, rv, rP, ry);
                 const float rc = sqrtf(k.gamma * rP * ry);
@@ -360,7 +387,7 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
                     for (int j = 0; j < 4; j++) Fr[j] = k.roe ? -101.0f : 0.5f * (F1[j] + F2[j]) - lam * (Rq[j] - L[j]);
                 }
                 float V[4] = {0.f, 0.f, 0.f, 0.f};
-                if (ns && order2) {   // first order never adds the viscous flux (res.cpp:27-29,50-53)
+                if (visc) {
                     float Aq[4];
 #pragma unroll
                     for (int j = 0; j < 4; j++) Aq[j] = 0.5f * (L[j] + Rq[j]);
@@ -369,17 +396,16 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
                     float ux = 0.f, uy = 0.f, vx = 0.f, vy = 0.f, Px = 0.f, Py = 0.f, rx = 0.f, rly = 0.f;
                     bool have = true;
                     if (s2 >= 0) {
-                        // l: unit vector c1 -> c2 (the LSQ displacement d1 - d2), m = (-ny, nx)
+                        // l: unit vector c1 -> c2 (the LSQ displacement d1 - d2)
                         const float tx = d1x - d2x, ty = d1y - d2y;
                         const float yd = rsqrtf(tx * tx + ty * ty);
-                        const float lxf = tx * yd, lyf = ty * yd, mxf = -fny, myf = fnx;
+                        const float lxf = tx * yd, lyf = ty * yd;
                         float dQx[4], dQy[4];
 #pragma unroll
                         for (int j = 0; j < 4; j++) {
-                            const float dl = (q2.p[j] - q1.p[j]) * yd;
-                            const float dm = 0.5f * (g1x.p[j] * mxf + g1y.p[j] * myf + g2x.p[j] * mxf + g2y.p[j] * myf);
-                            dQy[j] = (dl + dm) * lyf;   // reconstruction.cpp:138-146: l for both terms
-                            dQx[j] = (dl + dm) * lxf;
+                            const float dl = dq[j] * yd + dm[j];   // reconstruction.cpp:138-146: l for both terms
+                            dQy[j] = dl * lyf;
+                            dQx[j] = dl * lxf;
                         }
                         rx = dQx[0];
                         ux = dQx[1] - rx * au * ya;
@@ -391,9 +417,6 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
                         Py = k.gm1 * (dQy[3] - 0.5f * rly * (au * au + av * av) - arho * (au * uy + av * vy));
                     } else if (s2 == -4) {
                         const float ydn = rsqrtf(d1x * d1x + d1y * d1y);
-                        float cu, cv;
-                        if (init_prims) { cu = k.u_inf; cv = k.v_inf; }
-                        else { const float yq = 1.0f / q1.p[0]; cu = q1.p[1] * yq; cv = q1.p[2] * yq; }
                         const float dudn = -cu * ydn, dvdn = -cv * ydn;
                         ux = dudn * fnx; uy = dudn * fny;
                         vx = dvdn * fnx; vy = dvdn * fny;

@@ -146,6 +146,61 @@ void append_tile(const HostMesh& m, const DeviceLayout& L, const Tile& t, Marks&
 
 }  // namespace
 
+bool check_tile_layout(const TileLayout& T, const DeviceLayout& L, std::string& err) {
+    auto fail = [&](size_t t, const char* what) {
+        err = "tile " + std::to_string(t) + ": " + what;
+        return false;
+    };
+    long long cells = 0;
+    for (size_t t = 0; t < T.tiles.size(); t++) {
+        const TileRec& r = T.tiles[t];
+        const int ncell = r.ncore + r.n1 + r.n2, ngrad = r.ncore + r.n1;
+        if (r.ncore < 1 || r.ncore > kTileCore || ngrad > kTileGrad || ncell > kTileCells) return fail(t, "cell counts");
+        if (r.c0 != cells) return fail(t, "core cells not contiguous");
+        cells += r.ncore;
+        if (r.nrc > r.ngeo || r.ngeo > r.nr || r.nr > kTileRecs || r.ngeo > kTileGeo) return fail(t, "record counts");
+        if (r.nrp < r.nr || r.ngp < r.ngeo || (r.nrp & 3) || (r.ngp & 3) || 5 * r.nrp + 3 * r.ngp > 5 * kTileRecs + 3 * kTileGeo)
+            return fail(t, "record block shape");
+        if ((r.rec & 3) || (r.csr & 7) || (r.halo & 3) || (r.ncsr & 7) || (r.noff & 7) || (r.nhalo & 3) || r.ncsr > kTileCsr ||
+            r.noff < ngrad + 1 || r.noff > r.ncsr || r.nhalo < r.n1 + r.n2 || r.nhalo > kTileCells)
+            return fail(t, "block alignment or size");
+        if (r.rec + 5 * (long long)r.nrp + 3 * (long long)r.ngp > (long long)T.rec.size() ||
+            r.csr + r.ncsr > (long long)T.csr.size() || r.halo + r.nhalo > (long long)T.halo.size() ||
+            r.rbase + r.nr > (long long)T.qcell.size())
+            return fail(t, "block outside its array");
+        for (int h = 0; h < r.n1 + r.n2; h++) {
+            const int c = T.halo[r.halo + h];
+            if (c < 0 || c >= T.nc || (c >= r.c0 && c < r.c0 + r.ncore)) return fail(t, "halo id");
+        }
+        const uint32_t* b = T.rec.data() + r.rec;
+        for (int k = 0; k < r.nr; k++) {
+            const int s1 = (int)(b[k] & 0xFFFFu), s2 = (int)(int16_t)(b[k] >> 16);
+            // flux records read gradients (core and ring-1 cells); the others only states
+            const int lim = k < r.nrc ? ngrad : ncell;
+            if (s1 >= lim || s2 >= lim || s2 < -4) return fail(t, "record slot");
+            if (s2 < 0 && k >= r.ngeo) return fail(t, "boundary record without normal");
+            if (s2 == -4) {
+                const int q = T.qcell[r.rbase + k];
+                if (q < 0 || q >= T.nc) return fail(t, "no-slip ghost cell");
+            }
+        }
+        const uint16_t* off = T.csr.data() + r.csr;
+        const uint16_t* ent = off + r.noff;
+        if (off[0] != 0 || off[ngrad] > r.ncsr - r.noff) return fail(t, "csr offsets");
+        for (int g = 0; g < ngrad; g++) {
+            if (off[g + 1] < off[g]) return fail(t, "csr offsets");
+            const int c = g < r.ncore ? r.c0 + g : T.halo[r.halo + g - r.ncore];
+            if (off[g + 1] - off[g] != L.inc_off[c + 1] - L.inc_off[c]) return fail(t, "csr row length");
+            for (int e = off[g]; e < off[g + 1]; e++) {
+                const int rr = ent[e] >> 1;
+                if (rr >= r.nr || (g < r.ncore && rr >= r.nrc)) return fail(t, "csr entry");
+            }
+        }
+    }
+    if (cells != T.nc) { err = "tiles do not cover the cells"; return false; }
+    return true;
+}
+
 bool build_tile_layout(const HostMesh& m, const DeviceLayout& L, TileLayout& T, std::string& err) {
     T = TileLayout();
     const int nc = L.nc, nf = L.nf;
@@ -177,6 +232,7 @@ bool build_tile_layout(const HostMesh& m, const DeviceLayout& L, TileLayout& T, 
         todo.push_back({c0 + h, n - h});   // processed after the first half: tiles stay in cell order
         todo.push_back({c0, h});
     }
+    if (!check_tile_layout(T, L, err)) return false;
     T.rec_per_face = nf ? (double)recs / nf : 0.0;
     T.ring1_per_cell = nc ? (double)r1 / nc : 0.0;
     T.ring2_per_cell = nc ? (double)r2 / nc : 0.0;

@@ -82,5 +82,8 @@ struct DeviceLayout;
 // Build the tile layout of a mesh (device order from build_layout).  Returns false (with a
 // message) only if a single cell needs more than a tile's capacity.
 bool build_tile_layout(const HostMesh& m, const DeviceLayout& L, TileLayout& T, std::string& err);
+// Every index the stage kernels derive from the layout stays inside its array or shared-memory
+// region (run by build_tile_layout before a layout is used).
+bool check_tile_layout(const TileLayout& T, const DeviceLayout& L, std::string& err);
 
 }  // namespace fv2d

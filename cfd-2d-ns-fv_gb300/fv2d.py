@@ -25,7 +25,7 @@ GEOM = dict(area=20, nx=21, ny=22, fcx=23, fcy=24, c1dx=25, c1dy=26, c2dx=27, c2
 BC = {"FREESTREAM": -1, "SLIP_WALL": -2, "EXTRAPOLATION": -3, "NO_SLIP_WALL": -4}
 EXPORTS = [
     "fv2d_read_inputs", "fv2d_read_grid", "fv2d_write_grid", "fv2d_free", "fv2d_mesh_build", "fv2d_mesh_free", "fv2d_mesh_sizes",
-    "fv2d_mesh_get", "fv2d_mesh_permutation", "fv2d_create", "fv2d_create_from_files", "fv2d_destroy",
+    "fv2d_mesh_get", "fv2d_mesh_permutation", "fv2d_mesh_tiles", "fv2d_create", "fv2d_create_from_files", "fv2d_destroy",
     "fv2d_step", "fv2d_stage", "fv2d_set_state", "fv2d_load_state", "fv2d_get_state", "fv2d_get_field", "fv2d_residual_norm",
     "fv2d_sizes", "fv2d_save", "fv2d_post", "fv2d_write_history_headers", "fv2d_write_mesh_files",
     "fv2d_read_restart", "fv2d_write_restart", "fv2d_synchronize", "fv2d_set_store_residual", "fv2d_set_graphs", "fv2d_set_kernel_timing",
@@ -85,6 +85,7 @@ def library():
             "fv2d_mesh_sizes": (ctypes.c_int, [vp, ip]),
             "fv2d_mesh_get": (ctypes.c_int, [vp, ctypes.c_int, dp]),
             "fv2d_mesh_permutation": (ctypes.c_int, [vp, ctypes.c_int, ip]),
+            "fv2d_mesh_tiles": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_longlong)]),
             "fv2d_create": (ctypes.c_int, [ctypes.POINTER(MeshDesc), ctypes.POINTER(Case), ctypes.c_int, pvp]),
             "fv2d_create_from_files": (ctypes.c_int, [cp, ctypes.c_int, pvp]),
             "fv2d_destroy": (None, [vp]),
@@ -242,6 +243,13 @@ class HostMesh:
         out = np.empty(n, np.float64)
         _check(library().fv2d_mesh_get(self.h, fid, _dp(out)))
         return out
+
+    def tiles(self) -> dict:
+        """The FP32 engine's tile layout of this mesh (checked; host only)."""
+        o = (ctypes.c_longlong * 8)()
+        _check(library().fv2d_mesh_tiles(self.h, o))
+        keys = ("tiles", "record_words", "records", "csr_words", "halo_ids", "flux_records", "ring1", "ring2")
+        return dict(zip(keys, [int(v) for v in o]))
 
     def permutation(self, kind: int) -> np.ndarray:
         out = np.empty(self.nc if kind == 0 else self.nf, np.int32)

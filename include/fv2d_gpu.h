@@ -108,6 +108,11 @@ int fv2d_mesh_sizes(const fv2d_mesh* m, int* out8);
 int fv2d_mesh_get(const fv2d_mesh* m, int field, double* out);
 /* permutations: kind 0 = cell new->old (N), 1 = face new->old (F)                             */
 int fv2d_mesh_permutation(const fv2d_mesh* m, int kind, int* out);
+/* The FP32 engine's tile layout of a mesh (host only; no counterpart in the reference, whose
+ * solver has no device layout): builds it, checks that every index its stage kernels derive stays
+ * in range (FV2D_ERR_MESH otherwise) and reports tiles, record words, records, csr words, halo ids,
+ * face records with fluxes, ring-1 cells and ring-2 cells (out8).                               */
+int fv2d_mesh_tiles(const fv2d_mesh* m, long long* out8);
 
 /* ---- solver (GPU) ------------------------------------------------------------------------- */
 

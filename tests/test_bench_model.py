@@ -43,3 +43,18 @@ def test_single_solve_model_uses_stored_states_for_fp64_only():
     assert k32["k_gradient"] == bench.bytes_per_launch("k_gradient", N, F, NINC, NB, 4, True, True)
     # per cell-stage, the FP32 engine moves well under the FP64 one (half-width state, no stored states)
     assert sum(k32.values()) < 0.6 * sum(k64.values())
+
+
+def test_spec_bytes_per_cell_stage():
+    """The benchmark specification's algorithmic bytes: B = N(40.67 s + 28) + F(9 s + 8) + 4(2F - Nb)
+    per stage (Euler geometry), about 617 B (FP64) and 347 B (FP32) per cell-stage on a Voronoi mesh
+    with F = 3N; NS adds 5 s per face."""
+    import bench
+    N, F, Nb = 1_000_000, 3_000_000, 0
+    assert abs(bench.bytes_8d(N, F, Nb, 8) / N - 617.3) < 0.1
+    assert abs(bench.bytes_8d(N, F, Nb, 4) / N - 346.7) < 0.1
+    assert bench.bytes_8d(N, F, Nb, 4, ns=True) - bench.bytes_8d(N, F, Nb, 4) == 5 * 4 * F
+    assert bench.bytes_8d(N, F, Nb, 4, ns=True, euler_geometry=True) == bench.bytes_8d(N, F, Nb, 4)
+    out = bench.step_8d([(N, F, Nb, 4, False, True)], ms_per_iteration=3 * 0.1, peak=6763.0)
+    assert abs(out["bytes_per_cell_stage"] - 346.7) < 0.1
+    assert abs(out["achieved"] - 346.7 * N / 0.1e-3 / 1e9) < 1.0

@@ -226,3 +226,33 @@ def test_native_grid_writer_and_reader(pkg, tmp_path):
         np.testing.assert_array_equal(u, v)
     with pytest.raises(pkg.Fv2dError):
         pkg.fv2d.read_grid(str(tmp_path / "missing.in"))
+
+
+def golden_grid(pkg, name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    return pkg.meshgen.Grid(z["x"], z["y"], z["fp1"], z["fp2"], z["fc1"], z["fc2"], int(z["num_cells"]), name)
+
+
+@pytest.mark.parametrize("kind", ["voronoi", "cylinder", "quads", "wheels", "airfoil", "tiny"])
+def test_tile_layout_checks(pkg, kind):
+    """The FP32 engine's tile layout: built and checked on the host (every index its stage kernels
+    derive stays in range), with the duplication the design expects on Voronoi meshes."""
+    from conftest import wheels_grid
+    mg = pkg.meshgen
+    g = {"voronoi": lambda: mg.voronoi_bump_channel(60000, seed=2),
+         "cylinder": lambda: mg.voronoi_cylinder(12000, seed=0, box=(8.0, 4.0), h_wall=0.01, h_far=0.08),
+         "quads": lambda: mg.channel_bump_quads(128, 64),
+         "wheels": lambda: wheels_grid(pkg),
+         "airfoil": lambda: golden_grid(pkg, "airfoil_ns_sq_local"),
+         "tiny": lambda: mg.channel_bump_quads(4, 2)}[kind]()
+    case = dict(mg.DEFAULT_CASE, eqn="NS", BC1="NO_SLIP_WALL", BC2="FREESTREAM")
+    hm = pkg.HostMesh(g, pkg.case_from_dict(case))
+    t = hm.tiles()
+    assert t["tiles"] >= 1
+    assert g.num_faces <= t["flux_records"] <= 2 * g.num_faces
+    if kind == "voronoi":
+        # Morton tiles: a small share of the faces is evaluated by two tiles, and the halo rings
+        # hold about one cell per core cell
+        assert t["flux_records"] < 1.25 * g.num_faces
+        assert t["ring1"] + t["ring2"] < 1.3 * g.num_cells
+    hm.close()
