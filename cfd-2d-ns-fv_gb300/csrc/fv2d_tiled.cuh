@@ -98,6 +98,7 @@ __device__ __forceinline__ void tma_load(void* dst, const void* src, uint32_t by
 
 __device__ __forceinline__ float fw(uint32_t w) { return __uint_as_float(w); }
 
+
 // Primitives of a conservative state; returns 1/rho for later quotients.
 __device__ __forceinline__ void tprims(const float p[4], const Consts<float>& k, float& rho, float& u, float& v,
                                        float& P, float& y) {
@@ -116,7 +117,7 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
     int* shalo = reinterpret_cast<int*>(sm + kSmRec + kSmCsr);
     Q4<float>* cq = reinterpret_cast<Q4<float>*>(sm + kSmRec + kSmCsr + kSmHalo);
     Q4<float>* cg = reinterpret_cast<Q4<float>*>(sm + kSmRec + kSmCsr + kSmHalo + kSmCq);
-    __shared__ TileDesc td;
+    __shared__ TileDesc td, tdn;   // this tile, the next tile this CTA takes
     __shared__ TParams tp;
     __shared__ __align__(8) unsigned long long mbar;
     __shared__ int s_tile;
@@ -134,14 +135,21 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
     const Q4<float>* __restrict__ Gprev = a.G[(STAGE + 2) % 3];
     Q4<float>* __restrict__ Gout = a.G[STAGE];
 
+    // thread 0 takes each next tile while the current one is being processed: its index right
+    // after the current tile's copies are issued, its descriptor during the halo gather
+    int next_t = 0, tp_sid = -1;
+    if (tid == 0) {
+        next_t = atomicAdd(a.counter + STAGE, 1);
+        if (next_t < ntiles) tdn = a.tiles[next_t];
+    }
     for (;;) {
         if (tid == 0) {
-            int t = atomicAdd(a.counter + STAGE, 1);
+            int t = next_t;
             if (t >= ntiles) {
                 t = -1;
             } else {
-                td = a.tiles[t];
-                tp = a.P[td.sid];
+                td = tdn;
+                if (td.sid != tp_sid) { tp = a.P[td.sid]; tp_sid = td.sid; }
                 const TileDesc& d = td;
                 const bool ok = d.ncore > 0 && d.ncore <= kTileCore && d.ncore + d.n1 <= kTileGrad &&
                                 d.ncore + d.n1 + d.n2 <= kTileCells && d.nr <= kTileRecs && d.ngeo <= kTileGeo &&
@@ -152,6 +160,8 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
                 if (!ok) {
                     atomicOr(a.err, 4);
                     t = -2;
+                    next_t = atomicAdd(a.counter + STAGE, 1);
+                    if (next_t < ntiles) tdn = a.tiles[next_t];
                 } else {
                     // the previous tile's generic accesses of this shared memory are complete
                     // (barrier at the end of the loop); order them before the async-proxy writes
@@ -163,6 +173,7 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
                     tma_load(scsr, a.csr + d.csr, bcsr, mb);
                     if (bhal) tma_load(shalo, a.halo + d.halo, bhal, mb);
                     tma_load(cq, Qin + d.c0, bq, mb);
+                    next_t = atomicAdd(a.counter + STAGE, 1);
                 }
             }
             s_tile = t;
@@ -200,6 +211,7 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
             const int nh = order2 ? n1 + n2 : n1;
             for (int i = tid; i < nh; i += blockDim.x) cq[ncore + i] = Qin[cbase + shalo[i]];
         }
+        if (tid == 0 && next_t < ntiles) tdn = a.tiles[next_t];
         // the history flags act only on an iteration's first stage (STAGE 0); the second stage's
         // kernel, which does not read them, clears them for the next iteration
         if (STAGE == 1 && tid == 0) { a.P[td.sid].fresh = 0; a.P[td.sid].init_prims = 0; }
