@@ -410,7 +410,7 @@ private:
                 d.cbase = (int)s.c0; d.c0 = (int)(s.c0 + r.c0);
                 d.ncore = r.ncore; d.n1 = r.n1; d.n2 = r.n2;
                 d.nrc = r.nrc; d.ngeo = r.ngeo; d.nr = r.nr; d.nrp = r.nrp; d.ngp = r.ngp;
-                d.noff = r.noff; d.ncsr = r.ncsr; d.nhalo = r.nhalo; d.sid = sid;
+                d.noff = r.noff; d.ncsr = r.ncsr; d.nhalo = r.nhalo; d.sid = sid; d.ncc = r.ncc;
                 td.push_back(d);
             }
             sr[2 * sid + 1] = (int)td.size() - sr[2 * sid];

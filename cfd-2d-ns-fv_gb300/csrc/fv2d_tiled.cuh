@@ -25,11 +25,12 @@
 
 namespace fv2d {
 
-struct TParams {   // per solve
+struct __align__(16) TParams {   // per solve
     Consts<float> k;
     int order2, ns, squeeze, global_dt;
     int fresh, init_prims, pad0, pad1;
 };
+static_assert(sizeof(TParams) % 16 == 0, "TParams is copied in 16-byte pieces");
 
 struct TArgs {
     const TileDesc* tiles;
@@ -98,6 +99,18 @@ __device__ __forceinline__ void tma_load(void* dst, const void* src, uint32_t by
 
 __device__ __forceinline__ float fw(uint32_t w) { return __uint_as_float(w); }
 
+// Asynchronous copy of a 16-byte aligned object (a tile descriptor, a solve's parameters) to shared
+// memory; complete after cp.async.wait_all.
+template <class T>
+__device__ __forceinline__ void copy_async(T* dst, const T* src) {
+    static_assert(sizeof(T) % 16 == 0, "16-byte pieces");
+#pragma unroll
+    for (int i = 0; i < (int)(sizeof(T) / 16); i++)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst) + 16 * i),
+                     "l"(reinterpret_cast<const char*>(src) + 16 * i)
+                     : "memory");
+}
+
 
 // Primitives of a conservative state; returns 1/rho for later quotients.
 __device__ __forceinline__ void tprims(const float p[4], const Consts<float>& k, float& rho, float& u, float& v,
@@ -117,10 +130,11 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
     int* shalo = reinterpret_cast<int*>(sm + kSmRec + kSmCsr);
     Q4<float>* cq = reinterpret_cast<Q4<float>*>(sm + kSmRec + kSmCsr + kSmHalo);
     Q4<float>* cg = reinterpret_cast<Q4<float>*>(sm + kSmRec + kSmCsr + kSmHalo + kSmCq);
-    __shared__ TileDesc td, tdn;   // this tile, the next tile this CTA takes
-    __shared__ TParams tp;
+    __shared__ TileDesc td;
+    __shared__ __align__(16) TileDesc tdn;   // the next tile this CTA takes
+    __shared__ TParams tp, tpn;   // this tile's solve parameters, the next tile's
     __shared__ __align__(8) unsigned long long mbar;
-    __shared__ int s_tile;
+    __shared__ int s_tile, s_ctr[2];
     __shared__ float redf[kTileCore / 32];
     __shared__ double redd[4][kTileCore / 32];
 
@@ -135,9 +149,16 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
     const Q4<float>* __restrict__ Gprev = a.G[(STAGE + 2) % 3];
     Q4<float>* __restrict__ Gout = a.G[STAGE];
 
-    // thread 0 takes each next tile while the current one is being processed: its index right
-    // after the current tile's copies are issued, its descriptor during the halo gather
-    int next_t = 0, tp_sid = -1;
+    // thread 0 takes each next tile while the current one is being processed: its index during
+    // the halo gather (whose own loads cover the atomic's latency; a barrier waits for the
+    // thread's outstanding accesses), its descriptor by an asynchronous copy to shared memory
+    // issued in the next phase and awaited at the top of the loop; the solve's parameters are
+    // reloaded only when the solve changes
+    int next_t = 0, tp_sid = -1, tpn_sid = -1;
+    // the last stage's per-tile spectral maximum, folded into the solve's maximum by an atomic
+    // issued during the NEXT tile's gradients (or at the end), not before a barrier
+    float pend_max = -1.0f;
+    int pend_sid = 0;
     if (tid == 0) {
         next_t = atomicAdd(a.counter + STAGE, 1);
         if (next_t < ntiles) tdn = a.tiles[next_t];
@@ -148,12 +169,16 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
             if (t >= ntiles) {
                 t = -1;
             } else {
+                asm volatile("cp.async.wait_all;" ::: "memory");
                 td = tdn;
-                if (td.sid != tp_sid) { tp = a.P[td.sid]; tp_sid = td.sid; }
+                if (td.sid != tp_sid) {
+                    tp = td.sid == tpn_sid ? tpn : a.P[td.sid];
+                    tp_sid = td.sid;
+                }
                 const TileDesc& d = td;
                 const bool ok = d.ncore > 0 && d.ncore <= kTileCore && d.ncore + d.n1 <= kTileGrad &&
                                 d.ncore + d.n1 + d.n2 <= kTileCells && d.nr <= kTileRecs && d.ngeo <= kTileGeo &&
-                                d.nrc <= d.ngeo && d.ngeo <= d.nr && d.nrp >= d.nr && d.ngp >= d.ngeo &&
+                                d.ncc >= 0 && d.ncc <= d.nrc && d.nrc <= d.ngeo && d.ngeo <= d.nr && d.nrp >= d.nr && d.ngp >= d.ngeo &&
                                 5 * d.nrp + 3 * d.ngp <= kSmRecWords && d.ncsr <= kTileCsr && d.noff <= d.ncsr &&
                                 d.nhalo <= kTileCells && (d.nrp & 3) == 0 && (d.ngp & 3) == 0 && (d.ncsr & 7) == 0 &&
                                 (d.nhalo & 3) == 0 && (d.rec & 3) == 0 && (d.csr & 7) == 0 && (d.halo & 3) == 0;
@@ -173,14 +198,16 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
                     tma_load(scsr, a.csr + d.csr, bcsr, mb);
                     if (bhal) tma_load(shalo, a.halo + d.halo, bhal, mb);
                     tma_load(cq, Qin + d.c0, bq, mb);
-                    next_t = atomicAdd(a.counter + STAGE, 1);
                 }
             }
             s_tile = t;
         }
         __syncthreads();
         const int t = s_tile;
-        if (t == -1) break;
+        if (t == -1) {
+            if (STAGE == 2 && tid == 0 && pend_max >= 0.0f) atomic_max_pos(a.smax + pend_sid, pend_max);
+            break;
+        }
         if (t == -2) { __syncthreads(); continue; }
         const bool ok = mbar_wait(mb, parity);
         if (__syncthreads_or(!ok)) {
@@ -211,15 +238,15 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
             const int nh = order2 ? n1 + n2 : n1;
             for (int i = tid; i < nh; i += blockDim.x) cq[ncore + i] = Qin[cbase + shalo[i]];
         }
-        if (tid == 0 && next_t < ntiles) tdn = a.tiles[next_t];
+        if (tid == 0) next_t = atomicAdd(a.counter + STAGE, 1);
         // the history flags act only on an iteration's first stage (STAGE 0); the second stage's
         // kernel, which does not read them, clears them for the next iteration
         if (STAGE == 1 && tid == 0) { a.P[td.sid].fresh = 0; a.P[td.sid].init_prims = 0; }
         __syncthreads();
 
-        // ---- grad: limited LSQ gradients of the core and ring-1 cells
-        if (order2) {
-            for (int gI = tid; gI < ncore + n1; gI += blockDim.x) {
+        // ---- grad: the limited LSQ gradient of one core or ring-1 cell (local slot gI)
+        auto grad_cell = [&](int gI) {
+            {
                 const int gid = gI < ncore ? c0 + gI : cbase + shalo[gI - ncore];
                 const bool lim_prev = squeeze && !fresh;
                 // requested first: used only after the loop over the cell's faces
@@ -250,9 +277,8 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
                         const Q4<float> qn = cq[so];
 #pragma unroll
                         for (int j = 0; j < 4; j++) {
-                            d[j] = side ? qc.p[j] - qn.p[j] : qn.p[j] - qc.p[j];   // reference orientation c2 - c1
-                            qmin[j] = fminf(qmin[j], qn.p[j]);
-                            qmax[j] = fmaxf(qmax[j], qn.p[j]);
+                            d[j] = qn.p[j] - qc.p[j];
+                            if (squeeze) { qmin[j] = fminf(qmin[j], qn.p[j]); qmax[j] = fmaxf(qmax[j], qn.p[j]); }
                         }
                     } else if (so == -1) {
 #pragma unroll
@@ -279,7 +305,9 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
 #pragma unroll
                         for (int j = 0; j < 4; j++) d[j] = 0.f;
                     }
-                    const float fx = d1x - d2x, fy = d1y - d2y;   // LSQ displacement c1 -> c2 (or ghost)
+                    // LSQ displacement c1 -> c2 (or ghost), times Q(c2) - Q(c1): for a c2-side cell the
+                    // difference above is Q(c1) - Q(c2), so the displacement's sign is flipped instead
+                    const float fx = side ? d2x - d1x : d1x - d2x, fy = side ? d2y - d1y : d1y - d2y;
                     const float ox = side ? d2x : d1x, oy = side ? d2y : d1y;   // face centre - this cell
 #pragma unroll
                     for (int j = 0; j < 4; j++) {
@@ -315,18 +343,17 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
                 cg[2 * gI + 1] = gy;
                 if (gI < ncore) { Gout[2 * (size_t)gid] = gx; Gout[2 * (size_t)gid + 1] = gy; }
             }
-            __syncthreads();
-        }
+        };
 
-        // ---- flux: every face of a core cell; V*A - F*A (and the spectral term) replace its geometry
-        {
+        // ---- flux of one face of a core cell (record r); V*A - F*A (and the spectral term) replace
+        // its geometry rows
             float* w_t0 = reinterpret_cast<float*>(srec + nrp);
             float* w_t1 = reinterpret_cast<float*>(srec + 2 * nrp);
             float* w_t2 = reinterpret_cast<float*>(srec + 3 * nrp);
             float* w_t3 = reinterpret_cast<float*>(srec + 4 * nrp);
             float* w_sp = reinterpret_cast<float*>(srec + 5 * nrp);
             const bool visc = ns && order2;   // first order never adds the viscous flux (res.cpp:27-29,50-53)
-            for (int r = tid; r < td.nrc; r += blockDim.x) {
+            auto flux_rec = [&](int r) {
                 const uint32_t sl = r_sl[r];
                 const int s1 = (int)(sl & 0xFFFFu), s2 = (int)(int16_t)(sl >> 16);
                 const float d1x = r_d1x[r], d1y = r_d1y[r], d2x = r_d2x[r], d2y = r_d2y[r];
@@ -450,13 +477,53 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
                 w_t2[r] = (V[2] - Fr[2]) * A;
                 w_t3[r] = (V[3] - Fr[3]) * A;
                 if (STAGE == 2) w_sp[r] = k.roe ? (fabsf(k.vn0) + k.c0) * A : (fabsf(vna) + ca) * A;
+            };
+
+        // ---- schedule: core-cell gradients; then the ring-1 gradients on the first warps while the
+        // other warps take the fluxes of faces between two core cells (they need core gradients
+        // only); then every remaining flux.  Fluxes go to whole warps, 32 records at a time, from
+        // shared counters.
+        if (tid == 0) { s_ctr[0] = 0; s_ctr[1] = 0; }
+        if (order2) {
+            if (tid == 0 && next_t < ntiles) copy_async(&tdn, a.tiles + next_t);
+            if (STAGE == 2 && tid == 0 && pend_max >= 0.0f) { atomic_max_pos(a.smax + pend_sid, pend_max); pend_max = -1.0f; }
+            if (tid < ncore) grad_cell(tid);
+            __syncthreads();
+            if (tid == 0 && next_t < ntiles) {   // the next tile's solve parameters, if they change
+                asm volatile("cp.async.wait_all;" ::: "memory");
+                if (tdn.sid != tp_sid) { copy_async(&tpn, a.P + tdn.sid); tpn_sid = tdn.sid; }
+            }
+            const int w1 = (n1 + 31) >> 5;
+            if (warp < w1) {
+                if (tid < n1) grad_cell(ncore + tid);
+            } else {
+                for (;;) {
+                    int base = 0;
+                    if (lane == 0) base = atomicAdd(&s_ctr[0], 32);
+                    base = __shfl_sync(0xffffffffu, base, 0);
+                    if (base >= td.ncc) break;
+                    if (base + lane < td.ncc) flux_rec(base + lane);
+                }
+            }
+        } else if (tid == 0 && next_t < ntiles) {
+            copy_async(&tdn, a.tiles + next_t);
+        }
+        __syncthreads();
+        {
+            const int start = min(s_ctr[0], td.ncc), nrc = td.nrc;
+            for (;;) {
+                int base = 0;
+                if (lane == 0) base = start + atomicAdd(&s_ctr[1], 32);
+                base = __shfl_sync(0xffffffffu, base, 0);
+                if (base >= nrc) break;
+                if (base + lane < nrc) flux_rec(base + lane);
             }
         }
         __syncthreads();
 
         // ---- update: residual gather, time step, SSP-RK3 stage of the core cells
         float snext = 0.f;
-        double r2[4] = {0.0, 0.0, 0.0, 0.0};
+        float r2[4] = {0.f, 0.f, 0.f, 0.f};
         if (tid < ncore) {
             const int c = tid, gid = c0 + c;
             const float* t0 = reinterpret_cast<const float*>(srec + nrp);
@@ -514,24 +581,28 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
                 a.Qlo[gid] = lo;
                 a.S[gid] = snext;
 #pragma unroll
-                for (int j = 0; j < 4; j++) r2[j] = (double)r4[j] * (double)r4[j];
+                for (int j = 0; j < 4; j++) r2[j] = r4[j] * r4[j];
             }
             if (!positive(out.p[0]) || !positive(out.p[3])) atomicOr(a.flags + td.sid, 1);
         }
         if (STAGE == 2) {
-            // per tile: the spectral maximum (GLOBAL dt of the next iteration) and the residual sums
-            // of squares (the batch's per-solve norms), each reduced in a fixed order
+            // per tile: the spectral maximum (GLOBAL dt of the next iteration) and, for a batch, the
+            // residual sums of squares (its per-solve norms), each reduced in a fixed order: squares
+            // and per-warp sums in FP32, the warps' and tiles' sums in FP64 (GB300's FP64 unit is
+            // narrow: an FP64 reduction over every thread took longer than the whole update)
             float m = snext;
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) m = max2(m, __shfl_xor_sync(0xffffffffu, m, o));
+            if (a.tpart) {
 #pragma unroll
-            for (int j = 0; j < 4; j++)
+                for (int j = 0; j < 4; j++)
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) r2[j] += __shfl_xor_sync(0xffffffffu, r2[j], o);
+                    for (int o = 16; o > 0; o >>= 1) r2[j] += __shfl_xor_sync(0xffffffffu, r2[j], o);
+            }
             if (lane == 0) {
                 redf[warp] = m;
 #pragma unroll
-                for (int j = 0; j < 4; j++) redd[j][warp] = r2[j];
+                for (int j = 0; j < 4; j++) redd[j][warp] = (double)r2[j];
             }
             __syncthreads();
             if (tid == 0) {
@@ -541,7 +612,9 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
                     bm = max2(bm, redf[w]);
                     for (int j = 0; j < 4; j++) bs[j] += redd[j][w];
                 }
-                atomic_max_pos(a.smax + td.sid, bm);
+                if (pend_max >= 0.0f && pend_sid != td.sid) atomic_max_pos(a.smax + pend_sid, pend_max);
+                pend_max = (pend_max >= 0.0f && pend_sid == td.sid) ? max2(pend_max, bm) : bm;
+                pend_sid = td.sid;
                 if (a.tpart)
                     for (int j = 0; j < 4; j++) a.tpart[4 * (size_t)t + j] = bs[j];
             }

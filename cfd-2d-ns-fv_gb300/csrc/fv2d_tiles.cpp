@@ -31,7 +31,7 @@ struct Marks {
 struct Tile {
     int c0 = 0, ncore = 0;
     std::vector<int> ring1, ring2, faces;   // faces: new face ids in record order
-    int nrc = 0, ngeo = 0;
+    int ncc = 0, nrc = 0, ngeo = 0;
     std::vector<uint16_t> off, ent;          // csr offsets (ngrad + 1) and entries
 };
 
@@ -46,11 +46,23 @@ bool make_tile(const DeviceLayout& L, int c0, int n, int stamp, Marks& mk, Tile&
         mk.fstamp[f] = stamp;
         t.faces.push_back(f);
     };
-    // every face of a core cell (fluxes), in new face id order: interior faces first (the device
-    // order puts boundary faces after all interior faces), so warps do not mix the two branches
+    // every face of a core cell (fluxes): faces between two core cells first (their fluxes need
+    // only core gradients, so they can be evaluated while the ring-1 gradients are computed), then
+    // the other interior faces, then boundary faces (warps do not mix the boundary branches);
+    // new face id order within each group
     for (int c = c0; c < c0 + n; c++)
         for (int i = L.inc_off[c]; i < L.inc_off[c + 1]; i++) add_face(L.inc[i] >> 1);
-    std::sort(t.faces.begin(), t.faces.end());
+    auto group = [&](int f) {
+        const int a = L.fc1[f], b = L.fc2[f];
+        if (b < 0) return 2;
+        return (a >= c0 && a < c0 + n && b >= c0 && b < c0 + n) ? 0 : 1;
+    };
+    std::sort(t.faces.begin(), t.faces.end(), [&](int x, int y) {
+        const int gx = group(x), gy = group(y);
+        return gx != gy ? gx < gy : x < y;
+    });
+    t.ncc = 0;
+    while (t.ncc < (int)t.faces.size() && group(t.faces[t.ncc]) == 0) t.ncc++;
     t.nrc = (int)t.faces.size();
     // ring 1: the other cells of those faces
     for (int k = 0; k < t.nrc; k++) {
@@ -104,7 +116,7 @@ void append_tile(const HostMesh& m, const DeviceLayout& L, const Tile& t, Marks&
     (void)m;
     TileRec r;
     r.c0 = t.c0; r.ncore = t.ncore; r.n1 = (int)t.ring1.size(); r.n2 = (int)t.ring2.size();
-    r.nrc = t.nrc; r.ngeo = t.ngeo; r.nr = (int)t.faces.size();
+    r.ncc = t.ncc; r.nrc = t.nrc; r.ngeo = t.ngeo; r.nr = (int)t.faces.size();
     r.nrp = round_up(r.nr, 4); r.ngp = round_up(r.ngeo, 4);
     r.noff = round_up((int)t.off.size(), 8);
     r.ncsr = r.noff + round_up((int)t.ent.size(), 8);
@@ -158,7 +170,8 @@ bool check_tile_layout(const TileLayout& T, const DeviceLayout& L, std::string& 
         if (r.ncore < 1 || r.ncore > kTileCore || ngrad > kTileGrad || ncell > kTileCells) return fail(t, "cell counts");
         if (r.c0 != cells) return fail(t, "core cells not contiguous");
         cells += r.ncore;
-        if (r.nrc > r.ngeo || r.ngeo > r.nr || r.nr > kTileRecs || r.ngeo > kTileGeo) return fail(t, "record counts");
+        if (r.ncc < 0 || r.ncc > r.nrc || r.nrc > r.ngeo || r.ngeo > r.nr || r.nr > kTileRecs || r.ngeo > kTileGeo)
+            return fail(t, "record counts");
         if (r.nrp < r.nr || r.ngp < r.ngeo || (r.nrp & 3) || (r.ngp & 3) || 5 * r.nrp + 3 * r.ngp > 5 * kTileRecs + 3 * kTileGeo)
             return fail(t, "record block shape");
         if ((r.rec & 3) || (r.csr & 7) || (r.halo & 3) || (r.ncsr & 7) || (r.noff & 7) || (r.nhalo & 3) || r.ncsr > kTileCsr ||
@@ -176,8 +189,8 @@ bool check_tile_layout(const TileLayout& T, const DeviceLayout& L, std::string& 
         for (int k = 0; k < r.nr; k++) {
             const int s1 = (int)(b[k] & 0xFFFFu), s2 = (int)(int16_t)(b[k] >> 16);
             // flux records read gradients (core and ring-1 cells); the others only states
-            const int lim = k < r.nrc ? ngrad : ncell;
-            if (s1 >= lim || s2 >= lim || s2 < -4) return fail(t, "record slot");
+            const int lim = k < r.ncc ? r.ncore : k < r.nrc ? ngrad : ncell;
+            if (s1 >= lim || s2 >= lim || s2 < -4 || (k < r.ncc && s2 < 0)) return fail(t, "record slot");
             if (s2 < 0 && k >= r.ngeo) return fail(t, "boundary record without normal");
             if (s2 == -4) {
                 const int q = T.qcell[r.rbase + k];
