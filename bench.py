@@ -446,7 +446,7 @@ def measure_serving(pkg, args):
     t_pool = time.time() - t0
     stream = workloads.c5_stream(rate=args.serve_rate, duration=args.serve_seconds, seed=args.seed, lo=5e3, hi=2e6)
     budget = args.serve_budget_gb * 1e9
-    cells, faces, solves = serve.capacity_from_budget(pool, budget)
+    cells, faces, solves, bound = serve.capacity_from_budget(pool, budget)
     b = pkg.Batch(cells, faces, solves, precision=pkg.FP32)
     b.set_grid_mode(True)
     peak, _ = peaks()
@@ -467,7 +467,7 @@ def measure_serving(pkg, args):
             "stream": {"rate_per_s": args.serve_rate, "seconds": args.serve_seconds, "requests": len(stream),
                        "cells": "log-uniform 5k-2M (snapped to a pool of %d meshes)" % args.pool_meshes},
             "arena": {"budget_gb": args.serve_budget_gb, "cells": cells, "faces": faces, "bytes": usage["bytes"],
-                      "capped_by_32bit_face_ids": faces >= serve.MAX_ARENA_FACES},
+                      "bound": bound},
             "pool_gen_s": round(t_pool, 1)}
 
 

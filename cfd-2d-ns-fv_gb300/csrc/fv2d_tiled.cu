@@ -120,9 +120,8 @@ public:
         for (auto& p : pending_) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
         for (auto e : free_events_) cudaEventDestroy(e);
         if (arena_) cudaFree(arena_);
-        if (tile_pin_) cudaFreeHost(tile_pin_);
+        if (desc_pin_) cudaFreeHost(desc_pin_);
         if (pin_params_) cudaFreeHost(pin_params_);
-        if (tiles_free_) cudaEventDestroy(tiles_free_);
         if (stream_) cudaStreamDestroy(stream_);
     }
 
@@ -131,8 +130,13 @@ public:
         keep_r_ = keep_r;
         norms_ = norms;
         FV2D_T(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
-        FV2D_T(cudaEventCreateWithFlags(&tiles_free_, cudaEventDisableTiming));
         FV2D_T(cudaMallocHost(&pin_params_, sizeof(TParams) * (size_t)c.solves));
+        // page-locked mirrors of the tile descriptors, the per-solve tile ranges and the tile count:
+        // a solve's admission or removal copies only its own part
+        FV2D_T(cudaMallocHost(&desc_pin_, sizeof(TileDesc) * (size_t)c.tiles + 8 * (size_t)c.solves + 64));
+        sr_pin_ = (int*)((char*)desc_pin_ + sizeof(TileDesc) * (size_t)c.tiles);
+        cnt_pin_ = sr_pin_ + 2 * (size_t)c.solves;
+        std::memset(desc_pin_, 0, sizeof(TileDesc) * (size_t)c.tiles + 8 * (size_t)c.solves + 64);
         size_t off = 0;
         auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) & ~size_t(255); return o; };
         const size_t q4 = sizeof(Q4<float>), nc = (size_t)c.cells;
@@ -166,6 +170,7 @@ public:
         FV2D_T(cudaMemsetAsync(arena_, 0, bytes_, stream_));
         FV2D_T(cudaStreamSynchronize(stream_));
         cells_.reset(c.cells); recw_.reset(c.recw); recs_.reset(c.recs); csr_.reset(c.csr); halo_.reset(c.halo);
+        tiles_.reset(c.tiles);
         solves_.assign(c.solves, Solve());
         int dev = 0;
         FV2D_T(cudaGetDevice(&dev));
@@ -208,13 +213,14 @@ public:
         Solve s;
         s.n = im->nc; s.n4 = im->nc4; s.rw = im->recw; s.nq = im->nrec; s.ncs = im->ncsr; s.nh = im->nhalo;
         s.ntiles = (int)im->tiles.size();
-        if (ntiles_used_ + s.ntiles > caps_.tiles) { err = "batch tile capacity exhausted"; return FV2D_ERR_NOMEM; }
-        if (!cells_.alloc(s.n4, &s.c0)) { err = "batch cell capacity exhausted"; return FV2D_ERR_NOMEM; }
+        long long t0 = 0;
+        if (!tiles_.alloc(s.ntiles, &t0)) { err = "batch tile capacity exhausted"; return FV2D_ERR_NOMEM; }
+        s.first_tile = (int)t0;
+        if (!cells_.alloc(s.n4, &s.c0)) { tiles_.release(t0, s.ntiles); err = "batch cell capacity exhausted"; return FV2D_ERR_NOMEM; }
         if (!recw_.alloc(s.rw, &s.rw0)) { release(s, 1); err = "batch record capacity exhausted"; return FV2D_ERR_NOMEM; }
         if (!recs_.alloc(s.nq, &s.q0)) { release(s, 2); err = "batch record capacity exhausted"; return FV2D_ERR_NOMEM; }
         if (!csr_.alloc(s.ncs, &s.cs0)) { release(s, 3); err = "batch csr capacity exhausted"; return FV2D_ERR_NOMEM; }
         if (!halo_.alloc(s.nh, &s.h0)) { release(s, 4); err = "batch halo capacity exhausted"; return FV2D_ERR_NOMEM; }
-        ntiles_used_ += s.ntiles;
         // asynchronous copies from the page-locked image (kept alive by the solve record)
         const char* P = im->pin;
         auto up = [&](void* dst, size_t o, size_t bytes) {
@@ -239,12 +245,13 @@ public:
         fill(s, hi, lo);
         FV2D_T(cudaGetLastError());
         FV2D_T(cudaMemsetAsync(A_.flags + sid, 0, 4, stream_));
-        s.need_init = true;          // spectral sums once the solve's tiles are listed
+        s.need_init = true;          // spectral sums before the next step
         s.image = im;
         s.active = true;
         solves_[sid] = std::move(s);
+        rc = put_tiles(sid, true);
+        if (rc) return rc;
         *sid_out = sid;
-        tiles_dirty_ = true;
         return FV2D_OK;
     }
 
@@ -252,20 +259,16 @@ public:
         if (sid < 0 || sid >= caps_.solves || !solves_[sid].active) { err = "no such solve"; return FV2D_ERR_ARG; }
         FV2D_T(cudaStreamSynchronize(stream_));
         Solve& s = solves_[sid];
+        s.active = false;
+        int rc = put_tiles(sid, false);   // empty descriptors: the kernels skip these tiles
+        if (rc) return rc;
         release(s, 5);
-        ntiles_used_ -= s.ntiles;
         s = Solve();
-        tiles_dirty_ = true;
         return FV2D_OK;
     }
 
-    // Tile descriptors (and per-solve tile ranges) after admissions/removals, then the spectral
-    // sums of newly admitted solves.
+    // The spectral sums of newly admitted solves (before the next step).
     int prepare() {
-        if (tiles_dirty_) {
-            int rc = rebuild_tiles();
-            if (rc) return rc;
-        }
         for (int sid = 0; sid < caps_.solves; sid++) {
             Solve& s = solves_[sid];
             if (!s.active || !s.need_init) continue;
@@ -382,11 +385,11 @@ public:
     size_t bytes_ = 0;
     int sms_ = 1, grid_ = 1;
     std::string err;
-    RangeAlloc cells_, recw_, recs_, csr_, halo_;
+    RangeAlloc cells_, recw_, recs_, csr_, halo_, tiles_;
 
 private:
     void release(Solve& s, int upto) {
-        if (upto >= 1) cells_.release(s.c0, s.n4);
+        if (upto >= 1) { cells_.release(s.c0, s.n4); tiles_.release(s.first_tile, s.ntiles); }
         if (upto >= 2) recw_.release(s.rw0, s.rw);
         if (upto >= 3) recs_.release(s.q0, s.nq);
         if (upto >= 4) csr_.release(s.cs0, s.ncs);
@@ -395,46 +398,36 @@ private:
 
     void fill(const Solve& s, Q4<float> hi, Q4<float> lo);
 
-    int rebuild_tiles() {
-        tiles_dirty_ = false;
-        std::vector<TileDesc> td;
-        std::vector<int> sr(2 * (size_t)caps_.solves, 0);
-        for (int sid = 0; sid < caps_.solves; sid++) {
-            Solve& s = solves_[sid];
-            sr[2 * sid] = (int)td.size();
-            if (!s.active) continue;
-            s.first_tile = (int)td.size();
-            for (const TileRec& r : s.image->tiles) {
-                TileDesc d{};
-                d.rec = s.rw0 + r.rec; d.rbase = s.q0 + r.rbase; d.csr = s.cs0 + r.csr; d.halo = s.h0 + r.halo;
-                d.cbase = (int)s.c0; d.c0 = (int)(s.c0 + r.c0);
-                d.ncore = r.ncore; d.n1 = r.n1; d.n2 = r.n2;
-                d.nrc = r.nrc; d.ngeo = r.ngeo; d.nr = r.nr; d.nrp = r.nrp; d.ngp = r.ngp;
-                d.noff = r.noff; d.ncsr = r.ncsr; d.nhalo = r.nhalo; d.sid = sid; d.ncc = r.ncc;
-                td.push_back(d);
-            }
-            sr[2 * sid + 1] = (int)td.size() - sr[2 * sid];
+    // A solve's tile descriptors (arena offsets = its ranges' starts + the layout's solve-local
+    // offsets) written into its slots of the descriptor array, or zeroed (an empty tile, which the
+    // kernels skip) on removal; with its tile range (norms) and the descriptor count the kernels scan.
+    int put_tiles(int sid, bool active) {
+        const Solve& s = solves_[sid];
+        TileDesc* d = desc_pin_ + s.first_tile;
+        for (int i = 0; i < s.ntiles; i++) {
+            TileDesc& x = d[i];
+            x = TileDesc{};
+            if (!active) continue;
+            const TileRec& r = s.image->tiles[i];
+            x.rec = s.rw0 + r.rec; x.rbase = s.q0 + r.rbase; x.csr = s.cs0 + r.csr; x.halo = s.h0 + r.halo;
+            x.cbase = (int)s.c0; x.c0 = (int)(s.c0 + r.c0);
+            x.ncore = r.ncore; x.n1 = r.n1; x.n2 = r.n2;
+            x.nrc = r.nrc; x.ngeo = r.ngeo; x.nr = r.nr; x.nrp = r.nrp; x.ngp = r.ngp;
+            x.noff = r.noff; x.ncsr = r.ncsr; x.nhalo = r.nhalo; x.sid = sid; x.ncc = r.ncc;
         }
-        if ((long long)td.size() > caps_.tiles) { err = "tile list capacity exceeded"; return FV2D_ERR_NOMEM; }
-        const size_t bt = sizeof(TileDesc) * td.size(), bs = 4 * sr.size(), need = bt + bs + 64;
-        FV2D_T(cudaEventSynchronize(tiles_free_));   // the previous upload has been read
-        if (need > tile_pin_bytes_) {
-            if (tile_pin_) cudaFreeHost(tile_pin_);
-            tile_pin_ = nullptr;
-            tile_pin_bytes_ = 0;
-            FV2D_T(cudaMallocHost(&tile_pin_, 2 * need));
-            tile_pin_bytes_ = 2 * need;
-        }
-        int* cnt = (int*)tile_pin_;
-        cnt[0] = (int)td.size();
-        char* tp = tile_pin_ + 64;
-        if (bt) std::memcpy(tp, td.data(), bt);
-        std::memcpy(tp + bt, sr.data(), bs);
-        if (bt) FV2D_T(cudaMemcpyAsync((void*)A_.tiles, tp, bt, cudaMemcpyHostToDevice, stream_));
-        FV2D_T(cudaMemcpyAsync(srange_, tp + bt, bs, cudaMemcpyHostToDevice, stream_));
-        FV2D_T(cudaMemcpyAsync((void*)A_.ntiles, cnt, sizeof(int), cudaMemcpyHostToDevice, stream_));
-        FV2D_T(cudaEventRecord(tiles_free_, stream_));
-        ntiles_ = (int)td.size();
+        sr_pin_[2 * sid] = s.first_tile;
+        sr_pin_[2 * sid + 1] = active ? s.ntiles : 0;
+        long long hi = 0;
+        for (int k = 0; k < caps_.solves; k++)
+            if (solves_[k].active) hi = std::max<long long>(hi, (long long)solves_[k].first_tile + solves_[k].ntiles);
+        *cnt_pin_ = (int)hi;
+        if (s.ntiles)
+            FV2D_T(cudaMemcpyAsync((void*)(A_.tiles + s.first_tile), d, sizeof(TileDesc) * (size_t)s.ntiles,
+                                   cudaMemcpyHostToDevice, stream_));
+        FV2D_T(cudaMemcpyAsync(srange_ + 2 * sid, sr_pin_ + 2 * sid, 8, cudaMemcpyHostToDevice, stream_));
+        FV2D_T(cudaMemcpyAsync((void*)A_.ntiles, cnt_pin_, 4, cudaMemcpyHostToDevice, stream_));
+        // the count's mirror and this range are rewritten by later admissions or removals
+        FV2D_T(cudaStreamSynchronize(stream_));
         return FV2D_OK;
     }
 
@@ -457,13 +450,11 @@ private:
 
     void* arena_ = nullptr;
     int* srange_ = nullptr;
-    bool keep_r_ = false, norms_ = false, tiles_dirty_ = false, timing_ = false;
-    long long ntiles_used_ = 0;
-    int ntiles_ = 0;
+    bool keep_r_ = false, norms_ = false, timing_ = false;
     cudaGraphExec_t graph_ = nullptr;
-    char* tile_pin_ = nullptr;
-    size_t tile_pin_bytes_ = 0;
-    cudaEvent_t tiles_free_ = nullptr;
+    TileDesc* desc_pin_ = nullptr;   // page-locked mirrors: descriptors, tile ranges, tile count
+    int* sr_pin_ = nullptr;
+    int* cnt_pin_ = nullptr;
     TParams* pin_params_ = nullptr;
     std::vector<Pending> pending_;
     std::vector<cudaEvent_t> free_events_;

@@ -182,7 +182,11 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
                                 5 * d.nrp + 3 * d.ngp <= kSmRecWords && d.ncsr <= kTileCsr && d.noff <= d.ncsr &&
                                 d.nhalo <= kTileCells && (d.nrp & 3) == 0 && (d.ngp & 3) == 0 && (d.ncsr & 7) == 0 &&
                                 (d.nhalo & 3) == 0 && (d.rec & 3) == 0 && (d.csr & 7) == 0 && (d.halo & 3) == 0;
-                if (!ok) {
+                if (d.ncore == 0) {   // an empty slot (a removed solve's tiles)
+                    t = -2;
+                    next_t = atomicAdd(a.counter + STAGE, 1);
+                    if (next_t < ntiles) tdn = a.tiles[next_t];
+                } else if (!ok) {
                     atomicOr(a.err, 4);
                     t = -2;
                     next_t = atomicAdd(a.counter + STAGE, 1);

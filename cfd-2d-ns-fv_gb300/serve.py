@@ -271,13 +271,20 @@ def serve_one_at_a_time(stream, pool, duration, precision=fv2d.FP64, target=1e-6
                 target=target, max_iters=max_iters, check_every=check_every, stall_iters=stall_iters)
 
 
-MAX_ARENA_FACES = (1 << 29) - (1 << 20)    # face ids are 32-bit (face << 1 | side) in the arena
+# Arena limits: the FP64 batch stores arena face ids as 32-bit (face << 1 | side); the FP32 batch's
+# tile layout keeps solve-local ids and 64-bit block offsets, with 32-bit cell ids (<= 2^30 cells).
+MAX_ARENA_FACES = {fv2d.FP64: (1 << 29) - (1 << 20), fv2d.FP32: (1 << 31) - (1 << 24)}
+MAX_ARENA_CELLS = {fv2d.FP64: 1 << 30, fv2d.FP32: (1 << 30) - (1 << 20)}
 
 
 def capacity_from_budget(pool, budget_bytes, precision=fv2d.FP32):
     """Batch capacity (cells, faces, solves) whose arena fits in `budget_bytes`, in the proportion
-    of faces to cells of the pool's meshes, capped by the arena's 32-bit face ids."""
+    of faces to cells of the pool's meshes, within the arena's id limits; also which bound set it
+    ("budget" or "ids")."""
     per_cell = np.mean([fv2d.Batch.footprint(g, precision) / g.num_cells for g in pool.grids])
     faces_per_cell = float(np.mean([g.num_faces / g.num_cells for g in pool.grids]))
-    cells = int(min(budget_bytes / per_cell, MAX_ARENA_FACES / faces_per_cell))
-    return cells, int(cells * faces_per_cell) + 1024, max(16, min(8192, int(cells / 4000)))
+    by_budget = budget_bytes / per_cell
+    by_ids = min(MAX_ARENA_CELLS[precision], MAX_ARENA_FACES[precision] / faces_per_cell)
+    cells = int(min(by_budget, by_ids))
+    return (cells, int(cells * faces_per_cell) + 1024, max(16, min(8192, int(cells / 4000))),
+            "budget" if by_budget <= by_ids else "ids")
