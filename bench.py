@@ -486,7 +486,7 @@ def measure_precision(pkg, args):
                                                     check_every=100)
     first = dict(case, solution_poly_order=0, limiter="NONE")
     out["first_order"] = precision.compare(grid, first, drop=1e-6, max_iters=args.prec_max_iters_first,
-                                           check_every=200)
+                                           check_every=1000 if args.prec_max_iters_first > 50000 else 200)
     return out
 
 
