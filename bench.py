@@ -437,8 +437,9 @@ def measure_batched(pkg, args, peak, peak_kind):
 
 
 def measure_serving(pkg, args):
-    """c5 sample: a Poisson stream through continuous batching (FP32) and, as the baseline, the
-    same stream one request at a time through the plain FP64 path, each for `serve_seconds`."""
+    """c5 sample: a Poisson stream through continuous batching (FP32) for `serve_seconds` and, as the
+    baseline, the same stream one request at a time through the plain FP64 path for
+    `serve_baseline_seconds` (default: the same)."""
     from fv2d_gb300 import serve, workloads
     t0 = time.time()
     pool = serve.MeshPool(lo=5e3, hi=2e6, n=args.pool_meshes, seed=args.seed)
@@ -461,7 +462,8 @@ def measure_serving(pkg, args):
         out["step_8d_frac"] = round(out["bytes_per_s"] / 1e9 / peak, 4)
     usage = b.usage()
     b.close()
-    base = serve.serve_one_at_a_time(stream, pool, duration=args.serve_seconds, precision=pkg.FP64, target=1e-6,
+    base_s = args.serve_baseline_seconds if args.serve_baseline_seconds > 0 else args.serve_seconds
+    base = serve.serve_one_at_a_time(stream, pool, duration=base_s, precision=pkg.FP64, target=1e-6,
                                      max_iters=args.serve_max_iters, check_every=25, stall_iters=args.serve_stall_iters)
     return {"batched_fp32": out, "baseline_fp64_one_at_a_time": base,
             "stream": {"rate_per_s": args.serve_rate, "seconds": args.serve_seconds, "requests": len(stream),
@@ -682,6 +684,8 @@ def main():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=30.0)
     ap.add_argument("--serve-rate", type=float, default=50.0)
+    ap.add_argument("--serve-baseline-seconds", type=float, default=0.0,
+                    help="length of the one-at-a-time FP64 baseline stream (0: --serve-seconds)")
     ap.add_argument("--serve-budget-gb", type=float, default=8.0)
     ap.add_argument("--serve-max-iters", type=int, default=2000)
     ap.add_argument("--serve-stall-iters", type=int, default=250,

@@ -1,10 +1,13 @@
-"""Autotuner of the batched engine's tile shapes.
+"""Autotuner of the batched engine's launch shapes, per solve-size bucket.
 
-The batch kernels are persistent grids over tiles of `block * mult[bucket]` cells or faces of one
-solve (buckets split by solve size).  The tuner times whole iterations of the loaded batch (CUDA
-graph replay, wall clock around synchronised steps) for: first the block size with unit tiles,
-then each size bucket's tile multiple in turn, keeping the fastest.  Tile shapes never change
-results (the per-element code is the same), so tuning can run on the live batch.
+FP64 batches: persistent grids over tiles of `block * mult[bucket]` cells or faces of one solve;
+the tuner tries the block size with unit tiles, then each bucket's tile multiple in turn.
+FP32 batches (one fused kernel per RK stage over 256-cell tiles, one CTA of 256 threads per tile):
+the tile is fixed by the mesh layout; the tuner tries each bucket's faces per warp of the flux pass
+(flux records a warp takes per grab: 32 x mult) in turn.
+Both then try the grid mode (persistent CTAs against one CTA per tile).  The tuner times whole
+iterations of the loaded batch (CUDA graph replay, wall clock around synchronised steps) and keeps
+the fastest; launch shapes never change results, so tuning runs on the live batch.
 """
 from __future__ import annotations
 
@@ -23,10 +26,16 @@ def time_iterations(batch, iters=5, warmup=2):
     return (time.perf_counter() - t0) / iters
 
 
+FP32_MULTS = (1, 2, 4)          # faces per warp of the FP32 flux pass: 32, 64, 128
+
+
 def tune(batch, iters=5, warmup=2, blocks=BLOCKS, mults=MULTS, edges=None, log=None):
-    """Pick the fastest (block, tile_mult per bucket) for the solves currently in `batch`."""
+    """Pick the fastest (block, tile_mult per bucket, grid mode) for the solves currently in `batch`."""
+    from . import fv2d
     _, mult0, edges0 = batch.get_tuning()
     edges = tuple(edges or edges0)
+    if batch.precision == fv2d.FP32:
+        blocks, mults = (256,), FP32_MULTS   # the FP32 stage kernel's CTA is fixed at 256 threads
     batch.set_grid_mode(False)
     trials = []
     best = None

@@ -37,7 +37,7 @@ struct TiledImage {
     long long nc = 0, nc4 = 0, recw = 0, nrec = 0, ncsr = 0, nhalo = 0;
     double rec_per_face = 0, ring1 = 0, ring2 = 0;
     char* pin = nullptr;
-    size_t o_rec = 0, o_qc = 0, o_csr = 0, o_halo = 0, o_vol = 0, o_rvol = 0, o_ixx = 0, o_iyy = 0, o_ixy = 0;
+    size_t o_rec = 0, o_qc = 0, o_csr = 0, o_halo = 0, o_vol = 0, o_rvol = 0, o_lsq = 0;
     ~TiledImage() { if (pin) cudaFreeHost(pin); }
 };
 
@@ -56,14 +56,13 @@ int tiled_image(const HostMesh& hm, std::shared_ptr<TiledImage>& out, std::strin
     auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) & ~size_t(255); return o; };
     im->o_rec = take(4 * L.rec.size()); im->o_qc = take(4 * L.qcell.size()); im->o_csr = take(2 * L.csr.size());
     im->o_halo = take(4 * L.halo.size()); im->o_vol = take(4 * (size_t)L.nc4); im->o_rvol = take(4 * (size_t)L.nc4);
-    im->o_ixx = take(8 * (size_t)L.nc4); im->o_iyy = take(8 * (size_t)L.nc4); im->o_ixy = take(8 * (size_t)L.nc4);
+    im->o_lsq = take(16 * (size_t)L.nc4);
     FV2D_T(cudaMallocHost(&im->pin, off));
     auto cp = [&](size_t o, const void* src, size_t bytes) { if (bytes) std::memcpy(im->pin + o, src, bytes); };
     cp(im->o_rec, L.rec.data(), 4 * L.rec.size()); cp(im->o_qc, L.qcell.data(), 4 * L.qcell.size());
     cp(im->o_csr, L.csr.data(), 2 * L.csr.size()); cp(im->o_halo, L.halo.data(), 4 * L.halo.size());
     cp(im->o_vol, L.vol.data(), 4 * (size_t)L.nc4); cp(im->o_rvol, L.rvol.data(), 4 * (size_t)L.nc4);
-    cp(im->o_ixx, L.Ixx.data(), 8 * (size_t)L.nc4); cp(im->o_iyy, L.Iyy.data(), 8 * (size_t)L.nc4);
-    cp(im->o_ixy, L.Ixy.data(), 8 * (size_t)L.nc4);
+    cp(im->o_lsq, L.lsq.data(), 16 * (size_t)L.nc4);
     im->tiles = std::move(L.tiles);
     im->n2o = hm.cell_new2old;
     slot = im;
@@ -98,7 +97,7 @@ TiledCaps tiled_caps(long long cells, long long faces, int solves) {
 // Device bytes of those capacities (per-cell state and geometry, tile blocks, descriptors).
 long long tiled_bytes(const TiledCaps& c, bool keep_r) {
     const long long q4 = 16;
-    long long b = c.cells * (3 * q4 + 6 * q4 + 2 * q4 + (keep_r ? q4 : 0) + 4 * 4 + 3 * 8);
+    long long b = c.cells * (3 * q4 + 6 * q4 + 2 * q4 + (keep_r ? q4 : 0) + 4 * 4 + 16);
     b += 4 * c.recw + 4 * c.recs + 2 * c.csr + 4 * c.halo;
     b += (long long)sizeof(TileDesc) * c.tiles + 40LL * c.tiles;    // descriptors, norm partials
     b += (long long)c.solves * ((long long)sizeof(TParams) + 4 + 4 + 32 + 8);
@@ -111,6 +110,7 @@ public:
         bool active = false, need_init = false;
         long long c0 = 0, n = 0, n4 = 0, rw0 = 0, rw = 0, q0 = 0, nq = 0, cs0 = 0, ncs = 0, h0 = 0, nh = 0;
         int first_tile = 0, ntiles = 0, iterations = 0;
+        int fpw = 32;   // flux records a warp takes per grab in this solve's tiles
         std::shared_ptr<TiledImage> image;
     };
 
@@ -145,7 +145,7 @@ public:
         for (int i = 0; i < 3; i++) og[i] = take(2 * q4 * nc);
         const size_t oD = take(q4 * nc), olo = take(q4 * nc), oR = keep_r ? take(q4 * nc) : 0;
         const size_t odt = take(4 * nc), oS = take(4 * nc), ovol = take(4 * nc), orvol = take(4 * nc);
-        const size_t oixx = take(8 * nc), oiyy = take(8 * nc), oixy = take(8 * nc);
+        const size_t olsq = take(16 * nc);
         const size_t orec = take(4 * (size_t)c.recw), oqc = take(4 * (size_t)c.recs), ocsr = take(2 * (size_t)c.csr);
         const size_t ohalo = take(4 * (size_t)c.halo);
         const size_t otiles = take(sizeof(TileDesc) * (size_t)c.tiles), otpart = take(32 * (size_t)c.tiles);
@@ -158,7 +158,7 @@ public:
         for (int i = 0; i < 3; i++) { A_.Q[i] = (Q4<float>*)(a + oq[i]); A_.G[i] = (Q4<float>*)(a + og[i]); }
         A_.D = (Q4<float>*)(a + oD); A_.Qlo = (Q4<float>*)(a + olo); A_.R = keep_r ? (Q4<float>*)(a + oR) : nullptr;
         A_.dt = (float*)(a + odt); A_.S = (float*)(a + oS); A_.vol = (float*)(a + ovol); A_.rvol = (float*)(a + orvol);
-        A_.Ixx = (double*)(a + oixx); A_.Iyy = (double*)(a + oiyy); A_.Ixy = (double*)(a + oixy);
+        A_.lsq = (float4*)(a + olsq);
         A_.rec = (uint32_t*)(a + orec); A_.qcell = (int*)(a + oqc); A_.csr = (uint16_t*)(a + ocsr); A_.halo = (int*)(a + ohalo);
         A_.tiles = (TileDesc*)(a + otiles);
         A_.tpart = norms ? (double*)(a + otpart) : nullptr;
@@ -202,7 +202,7 @@ public:
         return p;
     }
 
-    int add(const HostMesh& hm, const fv2d_case& cs, int* sid_out) {
+    int add(const HostMesh& hm, const fv2d_case& cs, int* sid_out, int fpw = 32) {
         if (hm.bc1 != cs.bc1 || hm.bc2 != cs.bc2) { err = "mesh was built with other BC codes than this case"; return FV2D_ERR_ARG; }
         int sid = -1;
         for (int i = 0; i < caps_.solves; i++) if (!solves_[i].active) { sid = i; break; }
@@ -213,6 +213,7 @@ public:
         Solve s;
         s.n = im->nc; s.n4 = im->nc4; s.rw = im->recw; s.nq = im->nrec; s.ncs = im->ncsr; s.nh = im->nhalo;
         s.ntiles = (int)im->tiles.size();
+        s.fpw = fpw;
         long long t0 = 0;
         if (!tiles_.alloc(s.ntiles, &t0)) { err = "batch tile capacity exhausted"; return FV2D_ERR_NOMEM; }
         s.first_tile = (int)t0;
@@ -232,9 +233,7 @@ public:
         FV2D_T(up((void*)(A_.halo + s.h0), im->o_halo, 4 * (size_t)s.nh));
         FV2D_T(up((float*)A_.vol + s.c0, im->o_vol, 4 * (size_t)s.n4));
         FV2D_T(up((float*)A_.rvol + s.c0, im->o_rvol, 4 * (size_t)s.n4));
-        FV2D_T(up((double*)A_.Ixx + s.c0, im->o_ixx, 8 * (size_t)s.n4));
-        FV2D_T(up((double*)A_.Iyy + s.c0, im->o_iyy, 8 * (size_t)s.n4));
-        FV2D_T(up((double*)A_.Ixy + s.c0, im->o_ixy, 8 * (size_t)s.n4));
+        FV2D_T(up((void*)(A_.lsq + s.c0), im->o_lsq, 16 * (size_t)s.n4));
         pin_params_[sid] = params(cs);   // a slot is rewritten only after its solve was removed (synchronised)
         FV2D_T(cudaMemcpyAsync(A_.P + sid, pin_params_ + sid, sizeof(TParams), cudaMemcpyHostToDevice, stream_));
         // the uniform freestream state (main.cpp:75-118): hi = the state rounded to FP32, lo = the remainder
@@ -295,9 +294,11 @@ public:
         FV2D_T(cudaMemsetAsync(A_.counter + st, 0, 4, stream_));
         if (st == 2) FV2D_T(cudaMemsetAsync(A_.smax, 0, 4 * (size_t)caps_.solves, stream_));
         timed(st, [&] {
-            if (st == 0) k_tstage<0><<<grid_, kTileCore, kSmTotal, stream_>>>(A_);
-            else if (st == 1) k_tstage<1><<<grid_, kTileCore, kSmTotal, stream_>>>(A_);
-            else k_tstage<2><<<grid_, kTileCore, kSmTotal, stream_>>>(A_);
+            // persistent grid (CTAs that take tiles until none is left) or one CTA per tile slot
+            const int gr = full_grid_ ? (int)std::max<long long>(1, hi_tiles_) : grid_;
+            if (st == 0) k_tstage<0><<<gr, kTileCore, kSmTotal, stream_>>>(A_);
+            else if (st == 1) k_tstage<1><<<gr, kTileCore, kSmTotal, stream_>>>(A_);
+            else k_tstage<2><<<gr, kTileCore, kSmTotal, stream_>>>(A_);
         });
         FV2D_T(cudaGetLastError());
         if (st == 2 && norms_) {
@@ -360,6 +361,16 @@ public:
         return FV2D_OK;
     }
 
+    // Tuning (results do not depend on it): a solve's flux records per warp grab, the grid mode.
+    int set_fpw(int sid, int fpw) {
+        solves_[sid].fpw = fpw;
+        return put_tiles(sid, true);
+    }
+    void set_full_grid(bool full) {
+        if (full != full_grid_ && graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
+        full_grid_ = full;
+    }
+
     void set_timing(bool on) {
         timing_ = on;
         for (int i = 0; i < 3; i++) { ms_[i] = 0; launches_[i] = 0; }
@@ -384,6 +395,8 @@ public:
     cudaStream_t stream_ = nullptr;
     size_t bytes_ = 0;
     int sms_ = 1, grid_ = 1;
+    bool full_grid_ = false;
+    long long hi_tiles_ = 0;   // descriptor slots in use (up to the last active solve's)
     std::string err;
     RangeAlloc cells_, recw_, recs_, csr_, halo_, tiles_;
 
@@ -413,7 +426,7 @@ private:
             x.cbase = (int)s.c0; x.c0 = (int)(s.c0 + r.c0);
             x.ncore = r.ncore; x.n1 = r.n1; x.n2 = r.n2;
             x.nrc = r.nrc; x.ngeo = r.ngeo; x.nr = r.nr; x.nrp = r.nrp; x.ngp = r.ngp;
-            x.noff = r.noff; x.ncsr = r.ncsr; x.nhalo = r.nhalo; x.sid = sid; x.ncc = r.ncc;
+            x.noff = r.noff; x.ncsr = r.ncsr; x.nhalo = r.nhalo; x.sid = sid; x.ncc = r.ncc; x.fpw = s.fpw;
         }
         sr_pin_[2 * sid] = s.first_tile;
         sr_pin_[2 * sid + 1] = active ? s.ntiles : 0;
@@ -421,6 +434,8 @@ private:
         for (int k = 0; k < caps_.solves; k++)
             if (solves_[k].active) hi = std::max<long long>(hi, (long long)solves_[k].first_tile + solves_[k].ntiles);
         *cnt_pin_ = (int)hi;
+        if (full_grid_ && hi != hi_tiles_ && graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
+        hi_tiles_ = hi;
         if (s.ntiles)
             FV2D_T(cudaMemcpyAsync((void*)(A_.tiles + s.first_tile), d, sizeof(TileDesc) * (size_t)s.ntiles,
                                    cudaMemcpyHostToDevice, stream_));
@@ -700,7 +715,7 @@ public:
     }
 
     int add_mesh(const HostMesh& hm, const fv2d_case* cs, int* sid) override {
-        int rc = core_.add(hm, *cs, sid);
+        int rc = core_.add(hm, *cs, sid, fpw_for(hm.nc));
         if (rc) err_ = core_.err;
         return rc;
     }
@@ -757,13 +772,25 @@ public:
         return rc;
     }
 
-    // The FP32 engine's launch shape is fixed by its tile layout (256-cell tiles, one CTA of 256
-    // threads per tile, a persistent grid); the tuning is recorded and validated but changes nothing.
+    // The FP32 engine's tiles are fixed by its layout (up to 256 cells, one CTA of 256 threads per
+    // tile); its tuning is, per solve-size bucket, the faces per warp of the flux pass (flux records a
+    // warp takes per grab: 32 x tile_mult) and the grid mode (persistent CTAs, or one CTA per tile).
+    // `block` is validated and kept but does not change the launch.
     int set_tuning(const BatchTuning& t) override {
         if (t.block < 64 || t.block > 256 || (t.block & 31)) { err_ = "block must be a multiple of 32 in [64, 256]"; return FV2D_ERR_ARG; }
-        for (int b = 0; b < 3; b++) if (t.tile_mult[b] < 1 || t.tile_mult[b] > 64) { err_ = "tile multiple out of range"; return FV2D_ERR_ARG; }
+        for (int b = 0; b < 3; b++) if (t.tile_mult[b] < 1 || t.tile_mult[b] > 32) { err_ = "tile multiple out of range [1, 32]"; return FV2D_ERR_ARG; }
         tune_ = t;
+        core_.set_full_grid(t.full_grid != 0);
+        for (int sid = 0; sid < core_.caps_.solves; sid++) {
+            if (!core_.solves_[sid].active) continue;
+            const int rc = core_.set_fpw(sid, fpw_for(core_.solves_[sid].n));
+            if (rc) { err_ = core_.err; return rc; }
+        }
         return FV2D_OK;
+    }
+    int fpw_for(long long cells) const {
+        const int b = cells < tune_.bucket_edges[0] ? 0 : cells < tune_.bucket_edges[1] ? 1 : 2;
+        return 32 * tune_.tile_mult[b];
     }
     BatchTuning tuning() const override { return tune_; }
 

@@ -48,7 +48,7 @@ struct TArgs {
     Q4<float>* R;              // residual (null: not kept)
     float *dt, *S;
     const float *vol, *rvol;
-    const double *Ixx, *Iyy, *Ixy;
+    const float4* lsq;         // per cell: the LSQ inverse-moment terms (Ixx, Iyy, Ixy) rounded to FP32, 0
     float* smax;               // [solves] max spectral sum (GLOBAL dt)
     int* flags;                // [solves] non-physical state seen
     double* tpart;             // [tiles][4] residual sums of squares of the last stage (null: none)
@@ -133,16 +133,14 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
     __shared__ TileDesc td;
     __shared__ __align__(16) TileDesc tdn;   // the next tile this CTA takes
     __shared__ TParams tp, tpn;   // this tile's solve parameters, the next tile's
-    __shared__ __align__(8) unsigned long long mbar;
-    __shared__ int s_tile, s_ctr[2];
+    __shared__ __align__(8) unsigned long long mbar, mbar_h;
+    __shared__ int s_next, s_ctr[2];
     __shared__ float redf[kTileCore / 32];
     __shared__ double redd[4][kTileCore / 32];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const uint32_t mb = smem_u32(&mbar);
-    if (tid == 0) mbar_init(mb, 1);
-    __syncthreads();
-    uint32_t parity = 0;
+    const uint32_t mb = smem_u32(&mbar), mbh = smem_u32(&mbar_h);
+    uint32_t parity = 0, parity_h = 0;
     const int ntiles = *a.ntiles;
     const Q4<float>* __restrict__ Qin = a.Q[STAGE];
     const Q4<float>* __restrict__ Qprev = a.Q[(STAGE + 2) % 3];
@@ -152,101 +150,112 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
     // thread 0 takes each next tile while the current one is being processed: its index during
     // the halo gather (whose own loads cover the atomic's latency; a barrier waits for the
     // thread's outstanding accesses), its descriptor by an asynchronous copy to shared memory
-    // issued in the next phase and awaited at the top of the loop; the solve's parameters are
-    // reloaded only when the solve changes
+    // issued in the gradient pass; in the last flux pass (the halo list is free by then) it checks
+    // the descriptor and starts the copy of the next tile's halo list, so that the next tile's
+    // ring states are gathered while its other blocks are copied.  The solve's parameters are
+    // reloaded only when the solve changes.
     int next_t = 0, tp_sid = -1, tpn_sid = -1;
     // the last stage's per-tile spectral maximum, folded into the solve's maximum by an atomic
     // issued during the NEXT tile's gradients (or at the end), not before a barrier
     float pend_max = -1.0f;
     int pend_sid = 0;
+    // (thread 0) the next tile's fate in s_next: its index, -1 (none left) or -2 (an empty slot of
+    // a removed solve, or a descriptor out of range: skipped); for a tile, the halo copy on mbar_h,
+    // whose phase also publishes tdn to the threads that wait on it
+    auto decide = [&]() {
+        if (next_t >= ntiles) { s_next = -1; return; }
+        const TileDesc& d = tdn;
+        if (d.ncore == 0) { s_next = -2; return; }
+        const bool ok = d.ncore > 0 && d.ncore <= kTileCore && d.ncore + d.n1 <= kTileGrad &&
+                        d.ncore + d.n1 + d.n2 <= kTileCells && d.nr <= kTileRecs && d.ngeo <= kTileGeo &&
+                        d.ncc >= 0 && d.ncc <= d.nrc && d.nrc <= d.ngeo && d.ngeo <= d.nr && d.fpw >= 32 && d.fpw <= 1024 &&
+                        (d.fpw & 31) == 0 && d.nrp >= d.nr && d.ngp >= d.ngeo &&
+                        5 * d.nrp + 3 * d.ngp <= kSmRecWords && d.ncsr <= kTileCsr && d.noff <= d.ncsr &&
+                        d.n1 + d.n2 <= d.nhalo && d.nhalo <= kTileCells && (d.nrp & 3) == 0 && (d.ngp & 3) == 0 &&
+                        (d.ncsr & 7) == 0 && (d.nhalo & 3) == 0 && (d.rec & 3) == 0 && (d.csr & 7) == 0 && (d.halo & 3) == 0;
+        if (!ok) { atomicOr(a.err, 4); s_next = -2; return; }
+        // the earlier generic accesses of the halo list are complete (a barrier precedes every
+        // call); order them before the async-proxy writes
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        const uint32_t bhal = 4u * (uint32_t)d.nhalo;
+        mbar_expect_tx(mbh, bhal);
+        if (bhal) tma_load(shalo, a.halo + d.halo, bhal, mbh);
+        s_next = next_t;
+    };
     if (tid == 0) {
+        mbar_init(mb, 1);
+        mbar_init(mbh, 1);
         next_t = atomicAdd(a.counter + STAGE, 1);
         if (next_t < ntiles) tdn = a.tiles[next_t];
+        decide();
     }
+    __syncthreads();
     for (;;) {
-        if (tid == 0) {
-            int t = next_t;
-            if (t >= ntiles) {
-                t = -1;
-            } else {
-                asm volatile("cp.async.wait_all;" ::: "memory");
-                td = tdn;
-                if (td.sid != tp_sid) {
-                    tp = td.sid == tpn_sid ? tpn : a.P[td.sid];
-                    tp_sid = td.sid;
-                }
-                const TileDesc& d = td;
-                const bool ok = d.ncore > 0 && d.ncore <= kTileCore && d.ncore + d.n1 <= kTileGrad &&
-                                d.ncore + d.n1 + d.n2 <= kTileCells && d.nr <= kTileRecs && d.ngeo <= kTileGeo &&
-                                d.ncc >= 0 && d.ncc <= d.nrc && d.nrc <= d.ngeo && d.ngeo <= d.nr && d.nrp >= d.nr && d.ngp >= d.ngeo &&
-                                5 * d.nrp + 3 * d.ngp <= kSmRecWords && d.ncsr <= kTileCsr && d.noff <= d.ncsr &&
-                                d.nhalo <= kTileCells && (d.nrp & 3) == 0 && (d.ngp & 3) == 0 && (d.ncsr & 7) == 0 &&
-                                (d.nhalo & 3) == 0 && (d.rec & 3) == 0 && (d.csr & 7) == 0 && (d.halo & 3) == 0;
-                if (d.ncore == 0) {   // an empty slot (a removed solve's tiles)
-                    t = -2;
-                    next_t = atomicAdd(a.counter + STAGE, 1);
-                    if (next_t < ntiles) tdn = a.tiles[next_t];
-                } else if (!ok) {
-                    atomicOr(a.err, 4);
-                    t = -2;
-                    next_t = atomicAdd(a.counter + STAGE, 1);
-                    if (next_t < ntiles) tdn = a.tiles[next_t];
-                } else {
-                    // the previous tile's generic accesses of this shared memory are complete
-                    // (barrier at the end of the loop); order them before the async-proxy writes
-                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                    const uint32_t brec = 4u * (uint32_t)(5 * d.nrp + 3 * d.ngp), bcsr = 2u * (uint32_t)d.ncsr,
-                                   bhal = 4u * (uint32_t)d.nhalo, bq = 16u * (uint32_t)d.ncore;
-                    mbar_expect_tx(mb, brec + bcsr + bhal + bq);
-                    tma_load(srec, a.rec + d.rec, brec, mb);
-                    tma_load(scsr, a.csr + d.csr, bcsr, mb);
-                    if (bhal) tma_load(shalo, a.halo + d.halo, bhal, mb);
-                    tma_load(cq, Qin + d.c0, bq, mb);
-                }
-            }
-            s_tile = t;
-        }
-        __syncthreads();
-        const int t = s_tile;
+        const int t = s_next;
         if (t == -1) {
             if (STAGE == 2 && tid == 0 && pend_max >= 0.0f) atomic_max_pos(a.smax + pend_sid, pend_max);
             break;
         }
-        if (t == -2) { __syncthreads(); continue; }
-        const bool ok = mbar_wait(mb, parity);
+        if (t == -2) {
+            __syncthreads();   // every thread has read s_next
+            if (tid == 0) {
+                next_t = atomicAdd(a.counter + STAGE, 1);
+                if (next_t < ntiles) tdn = a.tiles[next_t];
+                decide();
+            }
+            __syncthreads();
+            continue;
+        }
+        if (tid == 0) {
+            td = tdn;
+            if (td.sid != tp_sid) {
+                tp = td.sid == tpn_sid ? tpn : a.P[td.sid];
+                tp_sid = td.sid;
+            }
+            // the previous tile's generic accesses of this shared memory are complete (barrier at
+            // the end of the loop); order them before the async-proxy writes
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            const TileDesc& d = td;
+            const uint32_t brec = 4u * (uint32_t)(5 * d.nrp + 3 * d.ngp), bcsr = 2u * (uint32_t)d.ncsr,
+                           bq = 16u * (uint32_t)d.ncore;
+            mbar_expect_tx(mb, brec + bcsr + bq);
+            tma_load(srec, a.rec + d.rec, brec, mb);
+            tma_load(scsr, a.csr + d.csr, bcsr, mb);
+            tma_load(cq, Qin + d.c0, bq, mb);
+        }
+        // ---- gather: the ring-1 and ring-2 states (after the halo copy; tdn is this tile's
+        // descriptor until thread 0 requests the next one, after the barrier below), while the
+        // other blocks are copied
+        bool ok = mbar_wait(mbh, parity_h);
+        parity_h ^= 1u;
+        if (ok) {
+            const int nh = tdn.n1 + tdn.n2, o = tdn.ncore, cb = tdn.cbase;
+            for (int i = tid; i < nh; i += blockDim.x) cq[o + i] = Qin[cb + shalo[i]];
+        }
+        if (tid == 0) next_t = atomicAdd(a.counter + STAGE, 1);
+        // the history flags act only on an iteration's first stage (STAGE 0); the second stage's
+        // kernel, which does not read them, clears them for the next iteration
+        if (STAGE == 1 && tid == 0) { a.P[td.sid].fresh = 0; a.P[td.sid].init_prims = 0; }
+        ok = mbar_wait(mb, parity) && ok;
+        parity ^= 1u;
         if (__syncthreads_or(!ok)) {
             if (tid == 0) atomicOr(a.err, 2);
             return;
         }
-        parity ^= 1u;
 
-        const int ncore = td.ncore, n1 = td.n1, n2 = td.n2, nrp = td.nrp, ngp = td.ngp;
+        const int ncore = td.ncore, n1 = td.n1, nrp = td.nrp, ngp = td.ngp;
         const int cbase = td.cbase, c0 = td.c0;
         const Consts<float>& k = tp.k;
         const bool order2 = tp.order2 != 0, ns = tp.ns != 0;
         const bool fresh = STAGE == 0 && tp.fresh != 0, init_prims = STAGE == 0 && tp.init_prims != 0;
         const bool squeeze = tp.squeeze != 0;
         const uint32_t* __restrict__ r_sl = srec;
-        const float* __restrict__ r_d1x = reinterpret_cast<const float*>(srec + nrp);
-        const float* __restrict__ r_d1y = reinterpret_cast<const float*>(srec + 2 * nrp);
-        const float* __restrict__ r_d2x = reinterpret_cast<const float*>(srec + 3 * nrp);
-        const float* __restrict__ r_d2y = reinterpret_cast<const float*>(srec + 4 * nrp);
+        const float4* __restrict__ r_d = reinterpret_cast<const float4*>(srec + nrp);
         const float* __restrict__ r_nx = reinterpret_cast<const float*>(srec + 5 * nrp);
         const float* __restrict__ r_ny = reinterpret_cast<const float*>(srec + 5 * nrp + ngp);
         const float* __restrict__ r_A = reinterpret_cast<const float*>(srec + 5 * nrp + 2 * ngp);
         const uint16_t* __restrict__ c_off = scsr;
         const uint16_t* __restrict__ c_ent = scsr + td.noff;
-
-        // ---- gather: ring-1 (and, for gradients, ring-2) states
-        {
-            const int nh = order2 ? n1 + n2 : n1;
-            for (int i = tid; i < nh; i += blockDim.x) cq[ncore + i] = Qin[cbase + shalo[i]];
-        }
-        if (tid == 0) next_t = atomicAdd(a.counter + STAGE, 1);
-        // the history flags act only on an iteration's first stage (STAGE 0); the second stage's
-        // kernel, which does not read them, clears them for the next iteration
-        if (STAGE == 1 && tid == 0) { a.P[td.sid].fresh = 0; a.P[td.sid].init_prims = 0; }
-        __syncthreads();
 
         // ---- grad: the limited LSQ gradient of one core or ring-1 cell (local slot gI)
         auto grad_cell = [&](int gI) {
@@ -254,7 +263,7 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
                 const int gid = gI < ncore ? c0 + gI : cbase + shalo[gI - ncore];
                 const bool lim_prev = squeeze && !fresh;
                 // requested first: used only after the loop over the cell's faces
-                const double dxx = a.Ixx[gid], dyy = a.Iyy[gid], dxy = a.Ixy[gid];
+                const float4 mom = a.lsq[gid];
                 Q4<float> qp, gpx, gpy;
                 if (lim_prev) { qp = Qprev[gid]; gpx = Gprev[2 * (size_t)gid]; gpy = Gprev[2 * (size_t)gid + 1]; }
                 const Q4<float> qc = cq[gI];
@@ -275,7 +284,8 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
                     const uint32_t sl = r_sl[r];
                     const int s1 = (int)(sl & 0xFFFFu), s2 = (int)(int16_t)(sl >> 16);
                     const int so = side ? s1 : s2;          // the face's other cell (or BC code)
-                    const float d1x = r_d1x[r], d1y = r_d1y[r], d2x = r_d2x[r], d2y = r_d2y[r];
+                    const float4 dd = r_d[r];
+                    const float d1x = dd.x, d1y = dd.y, d2x = dd.z, d2y = dd.w;
                     float d[4];
                     if (so >= 0) {
                         const Q4<float> qn = cq[so];
@@ -322,7 +332,7 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
                         tmax[j] = fmaxf(tmax[j], t);
                     }
                 }
-                const float ixx = (float)dxx, iyy = (float)dyy, ixy = (float)dxy;
+                const float ixx = mom.x, iyy = mom.y, ixy = mom.z;
                 Q4<float> gx, gy;
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
@@ -349,18 +359,16 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
             }
         };
 
-        // ---- flux of one face of a core cell (record r); V*A - F*A (and the spectral term) replace
-        // its geometry rows
-            float* w_t0 = reinterpret_cast<float*>(srec + nrp);
-            float* w_t1 = reinterpret_cast<float*>(srec + 2 * nrp);
-            float* w_t2 = reinterpret_cast<float*>(srec + 3 * nrp);
-            float* w_t3 = reinterpret_cast<float*>(srec + 4 * nrp);
+        // ---- flux of one face of a core cell (record r); V*A - F*A replaces its displacement row
+        // and the spectral term its normal's x
+            float4* w_t = reinterpret_cast<float4*>(srec + nrp);
             float* w_sp = reinterpret_cast<float*>(srec + 5 * nrp);
             const bool visc = ns && order2;   // first order never adds the viscous flux (res.cpp:27-29,50-53)
             auto flux_rec = [&](int r) {
                 const uint32_t sl = r_sl[r];
                 const int s1 = (int)(sl & 0xFFFFu), s2 = (int)(int16_t)(sl >> 16);
-                const float d1x = r_d1x[r], d1y = r_d1y[r], d2x = r_d2x[r], d2y = r_d2y[r];
+                const float4 dd = r_d[r];
+                const float d1x = dd.x, d1y = dd.y, d2x = dd.z, d2y = dd.w;
                 const float fnx = r_nx[r], fny = r_ny[r];
                 const float mxf = -fny, myf = fnx;   // unit tangent p1 -> p2
                 // face states; for NS also the face-average tangential derivative m.(grad Q1 + grad Q2)/2,
@@ -476,17 +484,15 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
                         V[3] = fnx * (au * txx + av * txy + k.k * dTx) + fny * (au * txy + av * tyy + k.k * dTy);
                     }
                 }
-                w_t0[r] = (V[0] - Fr[0]) * A;
-                w_t1[r] = (V[1] - Fr[1]) * A;
-                w_t2[r] = (V[2] - Fr[2]) * A;
-                w_t3[r] = (V[3] - Fr[3]) * A;
+                w_t[r] = make_float4((V[0] - Fr[0]) * A, (V[1] - Fr[1]) * A, (V[2] - Fr[2]) * A, (V[3] - Fr[3]) * A);
                 if (STAGE == 2) w_sp[r] = k.roe ? (fabsf(k.vn0) + k.c0) * A : (fabsf(vna) + ca) * A;
             };
 
         // ---- schedule: core-cell gradients; then the ring-1 gradients on the first warps while the
         // other warps take the fluxes of faces between two core cells (they need core gradients
-        // only); then every remaining flux.  Fluxes go to whole warps, 32 records at a time, from
-        // shared counters.
+        // only), which the first warps join when done; then every remaining flux.  Fluxes go to
+        // whole warps, td.fpw records at a time (the batch's faces-per-warp tuning), from shared
+        // counters.
         if (tid == 0) { s_ctr[0] = 0; s_ctr[1] = 0; }
         if (order2) {
             if (tid == 0 && next_t < ntiles) copy_async(&tdn, a.tiles + next_t);
@@ -497,30 +503,34 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
                 asm volatile("cp.async.wait_all;" ::: "memory");
                 if (tdn.sid != tp_sid) { copy_async(&tpn, a.P + tdn.sid); tpn_sid = tdn.sid; }
             }
-            const int w1 = (n1 + 31) >> 5;
-            if (warp < w1) {
-                if (tid < n1) grad_cell(ncore + tid);
-            } else {
+            // the first warps take the ring-1 gradients, then join the others on core-core fluxes
+            if (tid < n1) grad_cell(ncore + tid);
+            {
+                const int fpw = td.fpw, ncc = td.ncc;
                 for (;;) {
                     int base = 0;
-                    if (lane == 0) base = atomicAdd(&s_ctr[0], 32);
+                    if (lane == 0) base = atomicAdd(&s_ctr[0], fpw);
                     base = __shfl_sync(0xffffffffu, base, 0);
-                    if (base >= td.ncc) break;
-                    if (base + lane < td.ncc) flux_rec(base + lane);
+                    if (base >= ncc) break;
+                    for (int r = base + lane; r < min(base + fpw, ncc); r += 32) flux_rec(r);
                 }
             }
         } else if (tid == 0 && next_t < ntiles) {
             copy_async(&tdn, a.tiles + next_t);
         }
         __syncthreads();
+        if (tid == 0) {   // the next tile: its descriptor checked, its halo list copied (free now)
+            if (next_t < ntiles) asm volatile("cp.async.wait_all;" ::: "memory");
+            decide();
+        }
         {
-            const int start = min(s_ctr[0], td.ncc), nrc = td.nrc;
+            const int start = min(s_ctr[0], td.ncc), nrc = td.nrc, fpw = td.fpw;
             for (;;) {
                 int base = 0;
-                if (lane == 0) base = start + atomicAdd(&s_ctr[1], 32);
+                if (lane == 0) base = start + atomicAdd(&s_ctr[1], fpw);
                 base = __shfl_sync(0xffffffffu, base, 0);
                 if (base >= nrc) break;
-                if (base + lane < nrc) flux_rec(base + lane);
+                for (int r = base + lane; r < min(base + fpw, nrc); r += 32) flux_rec(r);
             }
         }
         __syncthreads();
@@ -530,10 +540,7 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
         float r2[4] = {0.f, 0.f, 0.f, 0.f};
         if (tid < ncore) {
             const int c = tid, gid = c0 + c;
-            const float* t0 = reinterpret_cast<const float*>(srec + nrp);
-            const float* t1 = reinterpret_cast<const float*>(srec + 2 * nrp);
-            const float* t2 = reinterpret_cast<const float*>(srec + 3 * nrp);
-            const float* t3 = reinterpret_cast<const float*>(srec + 4 * nrp);
+            const float4* tt = reinterpret_cast<const float4*>(srec + nrp);
             const float* sp = reinterpret_cast<const float*>(srec + 5 * nrp);
             // the stage's cell data, requested before the gather
             const float yv = a.rvol[gid];
@@ -548,10 +555,11 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
             const int e0 = c_off[c], e1 = c_off[c + 1];
             for (int e = e0; e < e1; e++) {
                 const int ent = c_ent[e], r = ent >> 1, side = ent & 1;
-                r4[0] += neg_if(t0[r], side);
-                r4[1] += neg_if(t1[r], side);
-                r4[2] += neg_if(t2[r], side);
-                r4[3] += neg_if(t3[r], side);
+                const float4 tv = tt[r];
+                r4[0] += neg_if(tv.x, side);
+                r4[1] += neg_if(tv.y, side);
+                r4[2] += neg_if(tv.z, side);
+                r4[3] += neg_if(tv.w, side);
                 if (STAGE == 2) snext += sp[r];
             }
 #pragma unroll

@@ -70,7 +70,13 @@ bool make_tile(const DeviceLayout& L, int c0, int n, int stamp, Marks& mk, Tile&
         for (int c : {L.fc1[f], L.fc2[f]})
             if (c >= 0 && mk.cstamp[c] != stamp) { mk.cstamp[c] = stamp; t.ring1.push_back(c); }
     }
-    std::sort(t.ring1.begin(), t.ring1.end());
+    // by face count, then id: the ring-1 gradient pass runs one cell per thread, so a warp's cells
+    // then loop over the same number of faces
+    auto nfaces = [&](int c) { return L.inc_off[c + 1] - L.inc_off[c]; };
+    std::sort(t.ring1.begin(), t.ring1.end(), [&](int x, int y) {
+        const int fx = nfaces(x), fy = nfaces(y);
+        return fx != fy ? fx < fy : x < y;
+    });
     for (size_t k = 0; k < t.ring1.size(); k++) mk.cslot[t.ring1[k]] = n + (int)k;
     // the other faces of ring-1 cells (their gradients): boundary faces first (they carry the
     // normal, which the slip-wall ghost needs), then interior faces
@@ -134,10 +140,11 @@ void append_tile(const HostMesh& m, const DeviceLayout& L, const Tile& t, Marks&
         const int s1 = slot(L.fc1[f]);
         const int s2 = L.fc2[f] >= 0 ? slot(L.fc2[f]) : L.fc2[f];
         b[k] = (uint32_t)(s1 & 0xFFFF) | ((uint32_t)(s2 & 0xFFFF) << 16);
-        b[r.nrp + k] = fbits(L.fgeo[3][f]);       // c1dx
-        b[2 * r.nrp + k] = fbits(L.fgeo[4][f]);   // c1dy
-        b[3 * r.nrp + k] = fbits(L.fgeo[5][f]);   // c2dx
-        b[4 * r.nrp + k] = fbits(L.fgeo[6][f]);   // c2dy
+        uint32_t* d = b + r.nrp + 4 * (size_t)k;   // one 16-byte row per record
+        d[0] = fbits(L.fgeo[3][f]);   // c1dx
+        d[1] = fbits(L.fgeo[4][f]);   // c1dy
+        d[2] = fbits(L.fgeo[5][f]);   // c2dx
+        d[3] = fbits(L.fgeo[6][f]);   // c2dy
         if (k < r.ngeo) {
             b[5 * r.nrp + k] = fbits(L.fgeo[0][f]);                 // nx
             b[5 * r.nrp + r.ngp + k] = fbits(L.fgeo[1][f]);         // ny
@@ -250,11 +257,11 @@ bool build_tile_layout(const HostMesh& m, const DeviceLayout& L, TileLayout& T, 
     T.ring1_per_cell = nc ? (double)r1 / nc : 0.0;
     T.ring2_per_cell = nc ? (double)r2 / nc : 0.0;
     T.vol.assign(T.nc4, 1.0f); T.rvol.assign(T.nc4, 1.0f);
-    T.Ixx.assign(T.nc4, 0.0); T.Iyy.assign(T.nc4, 0.0); T.Ixy.assign(T.nc4, 0.0);
+    T.lsq.assign(T.nc4, std::array<float, 4>{0.f, 0.f, 0.f, 0.f});
     for (int c = 0; c < nc; c++) {
         T.vol[c] = (float)L.vol[c];
         T.rvol[c] = (float)(1.0 / L.vol[c]);
-        T.Ixx[c] = L.Ixx[c]; T.Iyy[c] = L.Iyy[c]; T.Ixy[c] = L.Ixy[c];
+        T.lsq[c] = {(float)L.Ixx[c], (float)L.Iyy[c], (float)L.Ixy[c], 0.f};
     }
     return true;
 }

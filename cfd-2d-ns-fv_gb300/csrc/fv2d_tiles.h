@@ -11,10 +11,11 @@
 //           [ncore, ncore+n1) ring 1, [ncore+n1, ncore+n1+n2) ring 2; halo[] lists ring 1 then ring 2
 //   records one per face the tile needs: [0, nrc) every face of a core cell (fluxes are computed for
 //           these; the first ncc join two core cells), [nrc, ngeo) boundary faces of ring-1 cells,
-//           [ngeo, nr) the other faces of ring-1 cells (gradient only).  Record block, 4-byte words, SoA:
+//           [ngeo, nr) the other faces of ring-1 cells (gradient only).  Record block, 4-byte words:
 //             sl[nrp]   (s1 & 0xFFFF) | (s2 << 16): local slots of the face's c1 and c2 (s2 < 0: BC code)
-//             d1x[nrp] d1y[nrp] d2x[nrp] d2y[nrp]   face centre minus c1 / c2 centre (c2: ghost centre
-//                       for boundary faces), so the LSQ displacement is d1 - d2
+//             d[nrp][4] (d1x, d1y, d2x, d2y): face centre minus c1 / c2 centre (c2: ghost centre for
+//                       boundary faces), so the LSQ displacement is d1 - d2; one 16-byte row per
+//                       record, read (and, by the flux pass, overwritten) with one 128-bit access
 //             nx[ngp] ny[ngp] A[ngp]                normal and area of records [0, ngeo)
 //           nrp = nr and ngp = ngeo rounded up to 4 (16-byte rows)
 //   csr     u16 block: off[noff] (ngrad+1 offsets, padded to 8) then entries (record << 1 | side) of
@@ -24,6 +25,7 @@
 //           id, src/solver/cell_gradient.cpp:63-66), -1 otherwise
 #pragma once
 
+#include <array>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -59,7 +61,7 @@ struct TileDesc {
     int noff, ncsr, nhalo;
     int sid;
     int ncc;               // flux records joining two core cells (the first ncc)
-    int pad;
+    int fpw;               // flux records a warp takes per grab (a multiple of 32; the batch's tuning)
 };
 static_assert(sizeof(TileDesc) == 96, "TileDesc layout");
 
@@ -71,9 +73,10 @@ struct TileLayout {
     std::vector<int> qcell;              // per record
     std::vector<uint16_t> csr;           // csr blocks
     std::vector<int> halo;               // halo lists
-    // per cell, device order, nc4 entries: volume and its reciprocal (FP32), LSQ moments (FP64)
+    // per cell, device order, nc4 entries: volume and its reciprocal; the LSQ inverse-moment terms
+    // (Ixx, Iyy, Ixy, 0) rounded from FP64 to FP32 (the kernels' gradient reads one 16-byte row)
     std::vector<float> vol, rvol;
-    std::vector<double> Ixx, Iyy, Ixy;
+    std::vector<std::array<float, 4>> lsq;
     // statistics: records per face, ring-1 and ring-2 cells per cell
     double rec_per_face = 0, ring1_per_cell = 0, ring2_per_cell = 0;
 };

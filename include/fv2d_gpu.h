@@ -206,8 +206,11 @@ int fv2d_batch_step(fv2d_batch* b, int iterations);
 int fv2d_batch_norms(fv2d_batch* b, int* solve_ids, double* norms4, int* iterations, int max, int* n);
 int fv2d_batch_get_state(fv2d_batch* b, int solve_id, double* q);
 int fv2d_batch_synchronize(fv2d_batch* b);
-/* tile shape: threads per block (a multiple of 32 in [64, 256]), tile = block * tile_mult[bucket]
- * elements; buckets split at bucket_edges[0] and bucket_edges[1] cells                          */
+/* launch shape per solve-size bucket (buckets split at bucket_edges[0] and bucket_edges[1] cells);
+ * results never depend on it.  FP64: threads per block (a multiple of 32 in [64, 256]) and tiles
+ * of block * tile_mult[bucket] elements.  FP32 (fused stage kernel over the mesh's 256-cell tiles,
+ * 256 threads per tile): block is not used; tile_mult[bucket] in [1, 32] sets the faces per warp of
+ * the flux pass (32 * tile_mult flux records per grab).                                          */
 int fv2d_batch_set_tuning(fv2d_batch* b, int block, const int* tile_mult3, const int* bucket_edges2);
 int fv2d_batch_get_tuning(fv2d_batch* b, int* block, int* tile_mult3, int* bucket_edges2);
 /* grid of the stage kernels: 0 = persistent (SMs x resident blocks loop over the tiles),
