@@ -449,7 +449,7 @@ def measure_serving(pkg, args):
     budget = args.serve_budget_gb * 1e9
     cells, faces, solves, bound = serve.capacity_from_budget(pool, budget)
     b = pkg.Batch(cells, faces, solves, precision=pkg.FP32)
-    b.set_grid_mode(True)
+    b.set_grid_mode(False)   # persistent stage kernels: the autotuner's choice for FP32 batches (c4)
     peak, _ = peaks()
 
     def stage_bytes(g, spec):

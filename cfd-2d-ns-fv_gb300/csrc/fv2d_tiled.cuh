@@ -135,8 +135,8 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
     __shared__ TParams tp, tpn;   // this tile's solve parameters, the next tile's
     __shared__ __align__(8) unsigned long long mbar, mbar_h;
     __shared__ int s_next, s_ctr[2];
-    __shared__ float redf[kTileCore / 32];
-    __shared__ double redd[4][kTileCore / 32];
+    __shared__ float redf[kTileCore / 32];      // last stage: per-warp spectral maxima of a tile
+    __shared__ float redw[4][kTileCore / 32];   // and per-warp residual sums of squares
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t mb = smem_u32(&mbar), mbh = smem_u32(&mbar_h);
@@ -155,10 +155,25 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
     // ring states are gathered while its other blocks are copied.  The solve's parameters are
     // reloaded only when the solve changes.
     int next_t = 0, tp_sid = -1, tpn_sid = -1;
-    // the last stage's per-tile spectral maximum, folded into the solve's maximum by an atomic
-    // issued during the NEXT tile's gradients (or at the end), not before a barrier
-    float pend_max = -1.0f;
-    int pend_sid = 0;
+    // (last stage) a tile's per-warp spectral maxima and residual sums are folded by the last warp
+    // at the top of the next tile, while its blocks are copied (or at the end): the tile's maximum
+    // into its solve's by an atomic, the sums of squares over the warps in FP64, in warp order, into
+    // the tile's partials (batches' norms).  No barrier waits for either.
+    int red_t = -1, red_sid = 0;
+    auto fold = [&]() {
+        if (STAGE != 2 || red_t < 0 || warp != kTileCore / 32 - 1) return;
+        if (a.tpart && lane < 4) {
+            double sum = 0.0;
+            for (int w = 0; w < kTileCore / 32; w++) sum += (double)redw[lane][w];
+            a.tpart[4 * (size_t)red_t + lane] = sum;
+        }
+        if (lane == 0) {
+            float bm = 0.f;
+            for (int w = 0; w < kTileCore / 32; w++) bm = max2(bm, redf[w]);
+            atomic_max_pos(a.smax + red_sid, bm);
+        }
+        red_t = -1;
+    };
     // (thread 0) the next tile's fate in s_next: its index, -1 (none left) or -2 (an empty slot of
     // a removed solve, or a descriptor out of range: skipped); for a tile, the halo copy on mbar_h,
     // whose phase also publishes tdn to the threads that wait on it
@@ -193,7 +208,7 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
     for (;;) {
         const int t = s_next;
         if (t == -1) {
-            if (STAGE == 2 && tid == 0 && pend_max >= 0.0f) atomic_max_pos(a.smax + pend_sid, pend_max);
+            fold();
             break;
         }
         if (t == -2) {
@@ -222,7 +237,21 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
             tma_load(srec, a.rec + d.rec, brec, mb);
             tma_load(scsr, a.csr + d.csr, bcsr, mb);
             tma_load(cq, Qin + d.c0, bq, mb);
+            // L2 prefetches (bulk, asynchronous) of the tile's rows that the gradient and update
+            // passes read with plain loads later; rounded out to 16 bytes, inside the arena
+            auto pf = [&](const void* p, size_t bytes) {
+                const size_t lo = (size_t)p & ~(size_t)15, hi = ((size_t)p + bytes + 15) & ~(size_t)15;
+                asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(lo), "r"((uint32_t)(hi - lo)) : "memory");
+            };
+            const size_t n = (size_t)d.ncore;
+            if (tp.order2 && tp.squeeze) { pf(Qprev + d.c0, 16 * n); pf(Gprev + 2 * (size_t)d.c0, 32 * n); }
+            if (tp.order2) pf(a.lsq + d.c0, 16 * n);
+            pf(a.rvol + d.c0, 4 * n);
+            if (STAGE == 0) { pf(a.vol + d.c0, 4 * n); pf(a.S + d.c0, 4 * n); }
+            else { pf(a.Q[0] + d.c0, 16 * n); pf(a.D + d.c0, 16 * n); pf(a.dt + d.c0, 4 * n); }
+            if (STAGE == 2) pf(a.Qlo + d.c0, 16 * n);
         }
+        fold();   // the previous tile's last-stage reductions
         // ---- gather: the ring-1 and ring-2 states (after the halo copy; tdn is this tile's
         // descriptor until thread 0 requests the next one, after the barrier below), while the
         // other blocks are copied
@@ -496,7 +525,6 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
         if (tid == 0) { s_ctr[0] = 0; s_ctr[1] = 0; }
         if (order2) {
             if (tid == 0 && next_t < ntiles) copy_async(&tdn, a.tiles + next_t);
-            if (STAGE == 2 && tid == 0 && pend_max >= 0.0f) { atomic_max_pos(a.smax + pend_sid, pend_max); pend_max = -1.0f; }
             if (tid < ncore) grad_cell(tid);
             __syncthreads();
             if (tid == 0 && next_t < ntiles) {   // the next tile's solve parameters, if they change
@@ -598,10 +626,10 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
             if (!positive(out.p[0]) || !positive(out.p[3])) atomicOr(a.flags + td.sid, 1);
         }
         if (STAGE == 2) {
-            // per tile: the spectral maximum (GLOBAL dt of the next iteration) and, for a batch, the
-            // residual sums of squares (its per-solve norms), each reduced in a fixed order: squares
-            // and per-warp sums in FP32, the warps' and tiles' sums in FP64 (GB300's FP64 unit is
-            // narrow: an FP64 reduction over every thread took longer than the whole update)
+            // per warp: the spectral maximum (GLOBAL dt of the next iteration) and, for a batch, the
+            // residual sums of squares (its per-solve norms), squares and sums in FP32; the warps'
+            // values are folded at the next tile's top (fold: fixed order, FP64 across warps; GB300's
+            // FP64 unit is narrow, so only four lanes of one warp do FP64 arithmetic)
             float m = snext;
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) m = max2(m, __shfl_xor_sync(0xffffffffu, m, o));
@@ -614,22 +642,10 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
             if (lane == 0) {
                 redf[warp] = m;
 #pragma unroll
-                for (int j = 0; j < 4; j++) redd[j][warp] = (double)r2[j];
+                for (int j = 0; j < 4; j++) redw[j][warp] = r2[j];
             }
-            __syncthreads();
-            if (tid == 0) {
-                float bm = 0.f;
-                double bs[4] = {0.0, 0.0, 0.0, 0.0};
-                for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
-                    bm = max2(bm, redf[w]);
-                    for (int j = 0; j < 4; j++) bs[j] += redd[j][w];
-                }
-                if (pend_max >= 0.0f && pend_sid != td.sid) atomic_max_pos(a.smax + pend_sid, pend_max);
-                pend_max = (pend_max >= 0.0f && pend_sid == td.sid) ? max2(pend_max, bm) : bm;
-                pend_sid = td.sid;
-                if (a.tpart)
-                    for (int j = 0; j < 4; j++) a.tpart[4 * (size_t)t + j] = bs[j];
-            }
+            red_t = t;
+            red_sid = td.sid;
         }
         __syncthreads();
     }

@@ -48,10 +48,13 @@ def test_fp32_converged_density_error_first_order(pkg):
 
 def test_fp32_second_order_squeeze_fixed_iterations(pkg):
     """Second order with the squeeze limiter stalls short of a 1e-6 drop (the limiter reads the
-    previous stage's face values); compare the two precisions at an iteration cap."""
+    previous stage's face values); compare the two precisions at an iteration cap.  The bar is what
+    the FP32 engine holds here (rho L2 1.3e-4 measured), above the 1e-5 of a converged run: a face
+    value that crosses its bound flips the limiter factor (src/solver/squeeze.cpp:68-141), which
+    turns round-off differences into local O(1e-3) differences at the shocks."""
     from fv2d_gb300 import precision
     g = pkg.meshgen.voronoi_bump_channel(8000, seed=1)
     case = transonic_case(pkg)
     out = precision.compare(g, case, drop=1e-6, max_iters=1000, check_every=100)
     print(f"squeeze @1000 it: rho_l2={out['rho_l2']:.2e} P_l2={out['P_l2']:.2e} force={out['wall_force_rel_err']:.2e}")
-    assert out["rho_l2"] <= 1e-3, out["rho_l2"]
+    assert out["rho_l2"] <= 3e-4, out["rho_l2"]
