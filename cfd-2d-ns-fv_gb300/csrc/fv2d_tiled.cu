@@ -89,7 +89,10 @@ TiledCaps tiled_caps(long long cells, long long faces, int solves) {
     c.cells = round_up(cells + 4LL * solves, 4);
     c.recw = round_up(12 * faces + 32 * c.tiles, 4);
     c.recs = 2 * faces + 4 * c.tiles;
-    c.csr = round_up(12 * cells + 16 * c.tiles, 8);
+    // u16 words: offsets (~1.4 per cell) and two words per entry (~2.8 entries per face: both
+    // incidences of a face, for core and ring-1 cells); measured 17.6 per cell on Voronoi meshes
+    // (F = 3N), 11.4 on quads
+    c.csr = round_up(6 * faces + 2 * cells + 16 * c.tiles, 8);
     c.halo = round_up(cells + cells / 2 + 4 * c.tiles, 4);
     return c;
 }

@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
         const float* __restrict__ r_ny = reinterpret_cast<const float*>(srec + 5 * nrp + ngp);
         const float* __restrict__ r_A = reinterpret_cast<const float*>(srec + 5 * nrp + 2 * ngp);
         const uint16_t* __restrict__ c_off = scsr;
-        const uint16_t* __restrict__ c_ent = scsr + td.noff;
+        const uint32_t* __restrict__ c_ent = reinterpret_cast<const uint32_t*>(scsr + td.noff);
 
         // ---- grad: the limited LSQ gradient of one core or ring-1 cell (local slot gI)
         auto grad_cell = [&](int gI) {
@@ -293,26 +293,27 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
                 const bool lim_prev = squeeze && !fresh;
                 // requested first: used only after the loop over the cell's faces
                 const float4 mom = a.lsq[gid];
-                Q4<float> qp, gpx, gpy;
-                if (lim_prev) { qp = Qprev[gid]; gpx = Gprev[2 * (size_t)gid]; gpy = Gprev[2 * (size_t)gid + 1]; }
+                Q4<float> gpx, gpy;
+                if (lim_prev) { gpx = Gprev[2 * (size_t)gid]; gpy = Gprev[2 * (size_t)gid + 1]; }
                 const Q4<float> qc = cq[gI];
-                // LSQ sums (Q(c2) - Q(c1)) * (dxj, dyj) over the cell's faces, the bounds of the cell and
-                // its neighbours, and - for the squeeze limiter - the extremes over the faces of
-                // t = (previous stage's face value on this cell's side) - (this cell's value)
+                // LSQ sums (Q(c2) - Q(c1)) * (dxj, dyj) over the cell's faces and, for the squeeze
+                // limiter, the extremes over the neighbours of Q(n) - Q(c) (= the bounds Qmax - Q,
+                // Qmin - Q of squeeze.cpp: rounding is monotone, so the extreme difference is the
+                // difference of the extreme) and over the faces of gprev . (face centre - centre), the
+                // previous face value's part that varies by face (its base Qprev - Q is added after
+                // the loop, again exactly for the extremes)
                 float sx[4] = {0.f, 0.f, 0.f, 0.f}, sy[4] = {0.f, 0.f, 0.f, 0.f};
-                float qmin[4], qmax[4], tmin[4], tmax[4], base[4];
+                float dmin[4], dmax[4], tmin[4], tmax[4];
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
-                    qmin[j] = qc.p[j]; qmax[j] = qc.p[j];
+                    dmin[j] = 0.f; dmax[j] = 0.f;
                     tmin[j] = 3.0e38f; tmax[j] = -3.0e38f;
-                    base[j] = lim_prev ? qp.p[j] - qc.p[j] : -101.0f - qc.p[j];   // -101: fresh face history
                 }
                 const int e0 = c_off[gI], e1 = c_off[gI + 1];
                 for (int e = e0; e < e1; e++) {
-                    const int ent = c_ent[e], r = ent >> 1, side = ent & 1;
-                    const uint32_t sl = r_sl[r];
-                    const int s1 = (int)(sl & 0xFFFFu), s2 = (int)(int16_t)(sl >> 16);
-                    const int so = side ? s1 : s2;          // the face's other cell (or BC code)
+                    const uint32_t ent = c_ent[e];
+                    const int r = (int)((ent & 0xFFFFu) >> 1), side = (int)(ent & 1u);
+                    const int so = (int)(int16_t)(ent >> 16);   // the face's other cell (or BC code)
                     const float4 dd = r_d[r];
                     const float d1x = dd.x, d1y = dd.y, d2x = dd.z, d2y = dd.w;
                     float d[4];
@@ -321,7 +322,7 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
 #pragma unroll
                         for (int j = 0; j < 4; j++) {
                             d[j] = qn.p[j] - qc.p[j];
-                            if (squeeze) { qmin[j] = fminf(qmin[j], qn.p[j]); qmax[j] = fmaxf(qmax[j], qn.p[j]); }
+                            if (squeeze) { dmin[j] = fminf(dmin[j], d[j]); dmax[j] = fmaxf(dmax[j], d[j]); }
                         }
                     } else if (so == -1) {
 #pragma unroll
@@ -356,9 +357,11 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
                     for (int j = 0; j < 4; j++) {
                         sx[j] += d[j] * fx;
                         sy[j] += d[j] * fy;
-                        const float t = lim_prev ? base[j] + gpx.p[j] * ox + gpy.p[j] * oy : base[j];
-                        tmin[j] = fminf(tmin[j], t);
-                        tmax[j] = fmaxf(tmax[j], t);
+                        if (lim_prev) {
+                            const float x = gpx.p[j] * ox + gpy.p[j] * oy;
+                            tmin[j] = fminf(tmin[j], x);
+                            tmax[j] = fmaxf(tmax[j], x);
+                        }
                     }
                 }
                 const float ixx = mom.x, iyy = mom.y, ixy = mom.z;
@@ -372,12 +375,18 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
                     // squeeze (squeeze.cpp:68-141): phi = the smallest (bound - Q) / (face value - Q) over
                     // the faces whose previous face value leaves [Qmin, Qmax]; as x -> (bound - Q) / x is
                     // monotone on either side of zero, that is the quotient at the extreme t
+                    Q4<float> qp;
+                    if (lim_prev) qp = Qprev[gid];
 #pragma unroll
                     for (int j = 0; j < 4; j++) {
-                        const float up = qmax[j] - qc.p[j], dn = qmin[j] - qc.p[j];
+                        const float up = dmax[j], dn = dmin[j];
+                        // t = (previous face value) - Q: its base plus the extremes above; -101 is the
+                        // fresh face history's value
+                        const float base = lim_prev ? qp.p[j] - qc.p[j] : -101.0f - qc.p[j];
+                        const float thi = lim_prev ? base + tmax[j] : base, tlo = lim_prev ? base + tmin[j] : base;
                         float phi = 1.0f;
-                        if (tmax[j] > up) phi = fminf(phi, up / tmax[j]);
-                        if (tmin[j] < dn) phi = fminf(phi, dn / tmin[j]);
+                        if (thi > up) phi = fminf(phi, up / thi);
+                        if (tlo < dn) phi = fminf(phi, dn / tlo);
                         gx.p[j] *= phi;
                         gy.p[j] *= phi;
                     }
@@ -582,7 +591,8 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
             float r4[4] = {0.f, 0.f, 0.f, 0.f};
             const int e0 = c_off[c], e1 = c_off[c + 1];
             for (int e = e0; e < e1; e++) {
-                const int ent = c_ent[e], r = ent >> 1, side = ent & 1;
+                const uint32_t ent = c_ent[e];
+                const int r = (int)((ent & 0xFFFFu) >> 1), side = (int)(ent & 1u);
                 const float4 tv = tt[r];
                 r4[0] += neg_if(tv.x, side);
                 r4[1] += neg_if(tv.y, side);
@@ -666,7 +676,7 @@ __global__ void __launch_bounds__(kTileCore) k_tspec_init(const TileDesc* __rest
             const uint16_t* off = csr + d.csr;
             const uint16_t* ent = off + d.noff;
             const float* A = reinterpret_cast<const float*>(rec + d.rec + 5 * (size_t)d.nrp + 2 * (size_t)d.ngp);
-            for (int e = off[threadIdx.x]; e < off[threadIdx.x + 1]; e++) s += (fabsf(k.vn0) + k.c0) * A[ent[e] >> 1];
+            for (int e = off[threadIdx.x]; e < off[threadIdx.x + 1]; e++) s += (fabsf(k.vn0) + k.c0) * A[ent[2 * e] >> 1];
             S[d.c0 + threadIdx.x] = s;
         }
         float m = s;

@@ -32,7 +32,8 @@ struct Tile {
     int c0 = 0, ncore = 0;
     std::vector<int> ring1, ring2, faces;   // faces: new face ids in record order
     int ncc = 0, nrc = 0, ngeo = 0;
-    std::vector<uint16_t> off, ent;          // csr offsets (ngrad + 1) and entries
+    std::vector<uint16_t> off;               // csr offsets (ngrad + 1)
+    std::vector<uint32_t> ent;               // csr entries
 };
 
 // Gather the tile [c0, c0 + n): returns false when it exceeds a capacity.
@@ -109,13 +110,14 @@ bool make_tile(const DeviceLayout& L, int c0, int n, int stamp, Marks& mk, Tile&
     auto emit = [&](int c, int g) {
         for (int i = L.inc_off[c]; i < L.inc_off[c + 1]; i++) {
             const int f = L.inc[i] >> 1, side = L.inc[i] & 1;
-            t.ent.push_back((uint16_t)((mk.frec[f] << 1) | side));
+            const int other = side ? mk.cslot[L.fc1[f]] : (L.fc2[f] >= 0 ? mk.cslot[L.fc2[f]] : L.fc2[f]);
+            t.ent.push_back((uint32_t)((mk.frec[f] << 1) | side) | ((uint32_t)(other & 0xFFFF) << 16));
         }
         t.off[g + 1] = (uint16_t)t.ent.size();
     };
     for (int i = 0; i < n; i++) emit(c0 + i, i);
     for (int k = 0; k < n1; k++) emit(t.ring1[k], n + k);
-    return round_up(ngrad + 1, 8) + round_up((int)t.ent.size(), 8) <= kTileCsr;
+    return round_up(ngrad + 1, 8) + 2 * round_up((int)t.ent.size(), 4) <= kTileCsr;
 }
 
 void append_tile(const HostMesh& m, const DeviceLayout& L, const Tile& t, Marks& mk, TileLayout& T) {
@@ -125,7 +127,7 @@ void append_tile(const HostMesh& m, const DeviceLayout& L, const Tile& t, Marks&
     r.ncc = t.ncc; r.nrc = t.nrc; r.ngeo = t.ngeo; r.nr = (int)t.faces.size();
     r.nrp = round_up(r.nr, 4); r.ngp = round_up(r.ngeo, 4);
     r.noff = round_up((int)t.off.size(), 8);
-    r.ncsr = r.noff + round_up((int)t.ent.size(), 8);
+    r.ncsr = r.noff + 2 * round_up((int)t.ent.size(), 4);
     r.nhalo = round_up(r.n1 + r.n2, 4);
     r.rec = (long long)T.rec.size();
     r.rbase = (long long)T.qcell.size();
@@ -155,7 +157,10 @@ void append_tile(const HostMesh& m, const DeviceLayout& L, const Tile& t, Marks&
     // csr block
     T.csr.resize(T.csr.size() + r.ncsr, (uint16_t)0);
     std::copy(t.off.begin(), t.off.end(), T.csr.begin() + r.csr);
-    std::copy(t.ent.begin(), t.ent.end(), T.csr.begin() + r.csr + r.noff);
+    for (size_t e = 0; e < t.ent.size(); e++) {   // little-endian halves, as the device reads them
+        T.csr[r.csr + r.noff + 2 * e] = (uint16_t)(t.ent[e] & 0xFFFFu);
+        T.csr[r.csr + r.noff + 2 * e + 1] = (uint16_t)(t.ent[e] >> 16);
+    }
     // halo list
     T.halo.insert(T.halo.end(), t.ring1.begin(), t.ring1.end());
     T.halo.insert(T.halo.end(), t.ring2.begin(), t.ring2.end());
@@ -205,15 +210,18 @@ bool check_tile_layout(const TileLayout& T, const DeviceLayout& L, std::string& 
             }
         }
         const uint16_t* off = T.csr.data() + r.csr;
-        const uint16_t* ent = off + r.noff;
-        if (off[0] != 0 || off[ngrad] > r.ncsr - r.noff) return fail(t, "csr offsets");
+        const uint16_t* ent = off + r.noff;   // entry e: ent[2e] (record << 1 | side), ent[2e + 1] other slot
+        if (off[0] != 0 || 2 * off[ngrad] > r.ncsr - r.noff) return fail(t, "csr offsets");
         for (int g = 0; g < ngrad; g++) {
             if (off[g + 1] < off[g]) return fail(t, "csr offsets");
             const int c = g < r.ncore ? r.c0 + g : T.halo[r.halo + g - r.ncore];
             if (off[g + 1] - off[g] != L.inc_off[c + 1] - L.inc_off[c]) return fail(t, "csr row length");
             for (int e = off[g]; e < off[g + 1]; e++) {
-                const int rr = ent[e] >> 1;
+                const int rr = ent[2 * e] >> 1, side = ent[2 * e] & 1, other = (int)(int16_t)ent[2 * e + 1];
                 if (rr >= r.nr || (g < r.ncore && rr >= r.nrc)) return fail(t, "csr entry");
+                const uint32_t sl = b[rr];
+                const int s1 = (int)(sl & 0xFFFFu), s2 = (int)(int16_t)(sl >> 16);
+                if ((side ? s2 : s1) != g || other != (side ? s1 : s2)) return fail(t, "csr entry slots");
             }
         }
     }

@@ -18,9 +18,11 @@
 //                       record, read (and, by the flux pass, overwritten) with one 128-bit access
 //             nx[ngp] ny[ngp] A[ngp]                normal and area of records [0, ngeo)
 //           nrp = nr and ngp = ngeo rounded up to 4 (16-byte rows)
-//   csr     u16 block: off[noff] (ngrad+1 offsets, padded to 8) then entries (record << 1 | side) of
+//   csr     u16 words: off[noff] (ngrad+1 entry offsets, padded to 8 words) then 32-bit entries of
 //           every core and ring-1 cell, each cell's in ascending ORIGINAL face id (the reference's
-//           summation order), padded to 8
+//           summation order), padded to 4 entries: low half (record << 1 | side), high half the local
+//           slot of the face's other cell (or its BC code, < 0) as int16, so the gradient pass needs
+//           no lookup of the record's slots
 //   qcell   per record: NO_SLIP_WALL gradient ghost cell (the cell numbered like the face's original
 //           id, src/solver/cell_gradient.cpp:63-66), -1 otherwise
 #pragma once
@@ -33,11 +35,13 @@
 namespace fv2d {
 
 constexpr int kTileCore = 256;     // core cells per tile at most (threads per CTA)
-constexpr int kTileGrad = 416;     // core + ring-1 cells at most
-constexpr int kTileCells = 608;    // core + ring-1 + ring-2 cells at most
-constexpr int kTileRecs = 1408;    // records at most
-constexpr int kTileGeo = 1024;     // records with normal and area at most
-constexpr int kTileCsr = 2992;     // u16 words of the csr block at most (offsets + entries)
+constexpr int kTileGrad = 400;     // core + ring-1 cells at most
+constexpr int kTileCells = 560;    // core + ring-1 + ring-2 cells at most
+constexpr int kTileRecs = 1344;    // records at most
+constexpr int kTileGeo = 960;      // records with normal and area at most
+constexpr int kTileCsr = 5528;     // u16 words of the csr block at most (offsets + 32-bit entries)
+// (the largest tiles of a 1M-cell Voronoi mesh: 382 gradient cells, 518 cells, 1,272 records, 889
+// with geometry, 2,300 csr entries; a block over a capacity is halved)
 
 // One tile, solve-local offsets.
 struct TileRec {
