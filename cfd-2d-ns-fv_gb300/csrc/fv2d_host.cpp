@@ -343,16 +343,6 @@ void geometry(HostMesh& m) {
     }
 }
 
-// 2-D Morton key of a point quantised to 16 bits per axis.
-inline uint32_t spread16(uint32_t v) {
-    v &= 0xFFFFu;
-    v = (v | (v << 8)) & 0x00FF00FFu;
-    v = (v | (v << 4)) & 0x0F0F0F0Fu;
-    v = (v | (v << 2)) & 0x33333333u;
-    v = (v | (v << 1)) & 0x55555555u;
-    return v;
-}
-
 void renumber(HostMesh& m) {
     const int nc = m.nc, nf = m.nf;
     double x0 = m.ccx[0], x1 = m.ccx[0], y0 = m.ccy[0], y1 = m.ccy[0];
@@ -367,10 +357,19 @@ void renumber(HostMesh& m) {
         double qx = (m.ccx[c] - x0) * sc, qy = (m.ccy[c] - y0) * sc;
         uint32_t ix = (uint32_t)std::min(65535.0, std::max(0.0, std::isfinite(qx) ? qx : 0.0));
         uint32_t iy = (uint32_t)std::min(65535.0, std::max(0.0, std::isfinite(qy) ? qy : 0.0));
-        key[c] = ((uint64_t)(spread16(ix) | (spread16(iy) << 1)) << 32) | (uint32_t)c;
+        uint64_t d = 0;   // Hilbert index of (ix, iy) on a 65536^2 grid (xy -> d, quadrant by quadrant)
+        for (uint32_t s = 1u << 15; s > 0; s >>= 1) {
+            const uint32_t rx = (ix & s) ? 1u : 0u, ry = (iy & s) ? 1u : 0u;
+            d += (uint64_t)s * s * ((3u * rx) ^ ry);
+            if (ry == 0) {   // rotate the quadrant (the bits above s are not read again)
+                if (rx == 1) { ix = 65535u - ix; iy = 65535u - iy; }
+                std::swap(ix, iy);
+            }
+        }
+        key[c] = (d << 32) | (uint32_t)c;
     }
     std::sort(key.begin(), key.end());
-    // Within each run of kSideBlock Morton-consecutive cells (a small spatial patch), cells are
+    // Within each run of kSideBlock Hilbert-consecutive cells (a small spatial patch), cells are
     // ordered by face count (stable): a warp's cells then loop over the same number of faces, so
     // the per-cell gathers do not wait for the warp's one many-sided cell.  Results do not depend
     // on the order (every per-cell sum runs in ascending original face id).

@@ -1,6 +1,6 @@
 // Host-side mesh model of the GB300 fv2d library: input.in parsing, grid parsing, connectivity,
 // geometry (the reference's formulas, evaluated in the same operation order so FP64 results are
-// bit-identical when compiled with -ffp-contract=off) and the Morton renumbering that gives the
+// bit-identical when compiled with -ffp-contract=off) and the Hilbert renumbering that gives the
 // device its deterministic per-cell gathers.
 #pragma once
 

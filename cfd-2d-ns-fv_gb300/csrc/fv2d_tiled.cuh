@@ -195,6 +195,13 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
         const uint32_t bhal = 4u * (uint32_t)d.nhalo;
         mbar_expect_tx(mbh, bhal);
         if (bhal) tma_load(shalo, a.halo + d.halo, bhal, mbh);
+        {   // the tile's other blocks into L2 now, so that the copies at its top come from L2
+            const uint32_t brec = 4u * (uint32_t)(5 * d.nrp + 3 * d.ngp), bcsr = 2u * (uint32_t)d.ncsr,
+                           bq = 16u * (uint32_t)d.ncore;
+            asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a.rec + d.rec), "r"(brec) : "memory");
+            asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a.csr + d.csr), "r"(bcsr) : "memory");
+            asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(Qin + d.c0), "r"(bq) : "memory");
+        }
         s_next = next_t;
     };
     if (tid == 0) {

@@ -237,7 +237,7 @@ bool build_tile_layout(const HostMesh& m, const DeviceLayout& L, TileLayout& T, 
     Marks mk(nc, nf);
     int stamp = 0;
     Tile t;
-    // tiles are the renumbering's 256-cell Morton blocks; a block that exceeds a capacity (cells
+    // tiles are the renumbering's 256-cell Hilbert blocks; a block that exceeds a capacity (cells
     // with very many faces) is split in halves until it fits
     std::vector<std::pair<int, int>> todo;
     for (int c0 = nc - (nc - 1) % kTileCore - 1; c0 >= 0; c0 -= kTileCore) todo.push_back({c0, std::min(kTileCore, nc - c0)});

@@ -1,4 +1,4 @@
-// Tile layout of the FP32 engine: a mesh cut into tiles of up to kTileCore Morton-consecutive cells,
+// Tile layout of the FP32 engine: a mesh cut into tiles of up to kTileCore Hilbert-consecutive cells,
 // each tile carrying everything one RK stage of its cells needs in a few contiguous blocks, so that a
 // stage is ONE kernel: per tile it bulk-copies (TMA) the tile's blocks into shared memory, gathers
 // the states of its halo cells, computes the limited gradients of its core cells and of their
