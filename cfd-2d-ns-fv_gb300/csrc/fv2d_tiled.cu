@@ -429,7 +429,7 @@ private:
             x.cbase = (int)s.c0; x.c0 = (int)(s.c0 + r.c0);
             x.ncore = r.ncore; x.n1 = r.n1; x.n2 = r.n2;
             x.nrc = r.nrc; x.ngeo = r.ngeo; x.nr = r.nr; x.nrp = r.nrp; x.ngp = r.ngp;
-            x.noff = r.noff; x.ncsr = r.ncsr; x.nhalo = r.nhalo; x.sid = sid; x.ncc = r.ncc; x.fpw = s.fpw;
+            x.noff = r.noff; x.ncsr = r.ncsr; x.nhalo = r.nhalo; x.sid = sid; x.ncc = r.ncc; x.fpw = s.fpw; x.nint = r.nint;
         }
         sr_pin_[2 * sid] = s.first_tile;
         sr_pin_[2 * sid + 1] = active ? s.ntiles : 0;

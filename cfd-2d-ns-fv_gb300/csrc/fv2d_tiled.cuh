@@ -18,6 +18,7 @@
 #pragma once
 
 #include <cstdint>
+#include <type_traits>
 #include <cuda_runtime.h>
 
 #include "fv2d_kernels.cuh"
@@ -183,7 +184,7 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
         if (d.ncore == 0) { s_next = -2; return; }
         const bool ok = d.ncore > 0 && d.ncore <= kTileCore && d.ncore + d.n1 <= kTileGrad &&
                         d.ncore + d.n1 + d.n2 <= kTileCells && d.nr <= kTileRecs && d.ngeo <= kTileGeo &&
-                        d.ncc >= 0 && d.ncc <= d.nrc && d.nrc <= d.ngeo && d.ngeo <= d.nr && d.fpw >= 32 && d.fpw <= 1024 &&
+                        d.ncc >= 0 && d.ncc <= d.nint && d.nint <= d.nrc && d.nrc <= d.ngeo && d.ngeo <= d.nr && d.fpw >= 32 && d.fpw <= 1024 &&
                         (d.fpw & 31) == 0 && d.nrp >= d.nr && d.ngp >= d.ngeo &&
                         5 * d.nrp + 3 * d.ngp <= kSmRecWords && d.ncsr <= kTileCsr && d.noff <= d.ncsr &&
                         d.n1 + d.n2 <= d.nhalo && d.nhalo <= kTileCells && (d.nrp & 3) == 0 && (d.ngp & 3) == 0 &&
@@ -409,7 +410,10 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
             float4* w_t = reinterpret_cast<float4*>(srec + nrp);
             float* w_sp = reinterpret_cast<float*>(srec + 5 * nrp);
             const bool visc = ns && order2;   // first order never adds the viscous flux (res.cpp:27-29,50-53)
-            auto flux_rec = [&](int r) {
+            // INTERIOR (a compile-time tag): the record joins two cells, so the boundary branches go
+            // and both sides' reconstructions can be scheduled together
+            auto flux_rec = [&](int r, auto interior) {
+                constexpr bool INTERIOR = decltype(interior)::value;
                 const uint32_t sl = r_sl[r];
                 const int s1 = (int)(sl & 0xFFFFu), s2 = (int)(int16_t)(sl >> 16);
                 const float4 dd = r_d[r];
@@ -434,14 +438,14 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
                         dm[j] = g1x.p[j] * mxf + g1y.p[j] * myf;
                         dq[j] = -q1.p[j];
                     }
-                    if (visc && s2 == -4) {
+                    if (!INTERIOR && visc && s2 == -4) {
                         if (init_prims) { cu = k.u_inf; cv = k.v_inf; }
                         else { const float yq = 1.0f / q1.p[0]; cu = q1.p[1] * yq; cv = q1.p[2] * yq; }
                     }
                 }
                 float lrho, lu, lv, lP, ly;
                 tprims(L, k, lrho, lu, lv, lP, ly);
-                if (s2 >= 0) {
+                if (INTERIOR || s2 >= 0) {
                     const Q4<float> q2 = cq[s2];
                     Q4<float> g2x, g2y;
                     if (order2) { g2x = cg[2 * s2]; g2y = cg[2 * s2 + 1]; }
@@ -491,7 +495,7 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
                     tprims(Aq, k, arho, au, av, aP, ya);
                     float ux = 0.f, uy = 0.f, vx = 0.f, vy = 0.f, Px = 0.f, Py = 0.f, rx = 0.f, rly = 0.f;
                     bool have = true;
-                    if (s2 >= 0) {
+                    if (INTERIOR || s2 >= 0) {
                         // l: unit vector c1 -> c2 (the LSQ displacement d1 - d2)
                         const float tx = d1x - d2x, ty = d1y - d2y;
                         const float yd = rsqrtf(tx * tx + ty * ty);
@@ -556,7 +560,7 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
                     if (lane == 0) base = atomicAdd(&s_ctr[0], fpw);
                     base = __shfl_sync(0xffffffffu, base, 0);
                     if (base >= ncc) break;
-                    for (int r = base + lane; r < min(base + fpw, ncc); r += 32) flux_rec(r);
+                    for (int r = base + lane; r < min(base + fpw, ncc); r += 32) flux_rec(r, std::true_type{});
                 }
             }
         } else if (tid == 0 && next_t < ntiles) {
@@ -568,13 +572,16 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
             decide();
         }
         {
-            const int start = min(s_ctr[0], td.ncc), nrc = td.nrc, fpw = td.fpw;
+            const int start = min(s_ctr[0], td.ncc), nrc = td.nrc, fpw = td.fpw, nint = td.nint;
             for (;;) {
                 int base = 0;
                 if (lane == 0) base = start + atomicAdd(&s_ctr[1], fpw);
                 base = __shfl_sync(0xffffffffu, base, 0);
                 if (base >= nrc) break;
-                for (int r = base + lane; r < min(base + fpw, nrc); r += 32) flux_rec(r);
+                for (int r = base + lane; r < min(base + fpw, nrc); r += 32) {
+                    if (r < nint) flux_rec(r, std::true_type{});
+                    else flux_rec(r, std::false_type{});
+                }
             }
         }
         __syncthreads();

@@ -31,7 +31,7 @@ struct Marks {
 struct Tile {
     int c0 = 0, ncore = 0;
     std::vector<int> ring1, ring2, faces;   // faces: new face ids in record order
-    int ncc = 0, nrc = 0, ngeo = 0;
+    int ncc = 0, nint = 0, nrc = 0, ngeo = 0;
     std::vector<uint16_t> off;               // csr offsets (ngrad + 1)
     std::vector<uint32_t> ent;               // csr entries
 };
@@ -64,6 +64,8 @@ bool make_tile(const DeviceLayout& L, int c0, int n, int stamp, Marks& mk, Tile&
     });
     t.ncc = 0;
     while (t.ncc < (int)t.faces.size() && group(t.faces[t.ncc]) == 0) t.ncc++;
+    t.nint = t.ncc;
+    while (t.nint < (int)t.faces.size() && group(t.faces[t.nint]) == 1) t.nint++;
     t.nrc = (int)t.faces.size();
     // ring 1: the other cells of those faces
     for (int k = 0; k < t.nrc; k++) {
@@ -124,7 +126,7 @@ void append_tile(const HostMesh& m, const DeviceLayout& L, const Tile& t, Marks&
     (void)m;
     TileRec r;
     r.c0 = t.c0; r.ncore = t.ncore; r.n1 = (int)t.ring1.size(); r.n2 = (int)t.ring2.size();
-    r.ncc = t.ncc; r.nrc = t.nrc; r.ngeo = t.ngeo; r.nr = (int)t.faces.size();
+    r.ncc = t.ncc; r.nint = t.nint; r.nrc = t.nrc; r.ngeo = t.ngeo; r.nr = (int)t.faces.size();
     r.nrp = round_up(r.nr, 4); r.ngp = round_up(r.ngeo, 4);
     r.noff = round_up((int)t.off.size(), 8);
     r.ncsr = r.noff + 2 * round_up((int)t.ent.size(), 4);
@@ -182,7 +184,7 @@ bool check_tile_layout(const TileLayout& T, const DeviceLayout& L, std::string& 
         if (r.ncore < 1 || r.ncore > kTileCore || ngrad > kTileGrad || ncell > kTileCells) return fail(t, "cell counts");
         if (r.c0 != cells) return fail(t, "core cells not contiguous");
         cells += r.ncore;
-        if (r.ncc < 0 || r.ncc > r.nrc || r.nrc > r.ngeo || r.ngeo > r.nr || r.nr > kTileRecs || r.ngeo > kTileGeo)
+        if (r.ncc < 0 || r.ncc > r.nint || r.nint > r.nrc || r.nrc > r.ngeo || r.ngeo > r.nr || r.nr > kTileRecs || r.ngeo > kTileGeo)
             return fail(t, "record counts");
         if (r.nrp < r.nr || r.ngp < r.ngeo || (r.nrp & 3) || (r.ngp & 3) || 5 * r.nrp + 3 * r.ngp > 5 * kTileRecs + 3 * kTileGeo)
             return fail(t, "record block shape");
@@ -203,6 +205,7 @@ bool check_tile_layout(const TileLayout& T, const DeviceLayout& L, std::string& 
             // flux records read gradients (core and ring-1 cells); the others only states
             const int lim = k < r.ncc ? r.ncore : k < r.nrc ? ngrad : ncell;
             if (s1 >= lim || s2 >= lim || s2 < -4 || (k < r.ncc && s2 < 0)) return fail(t, "record slot");
+            if (k < r.nrc && (k < r.nint) != (s2 >= 0)) return fail(t, "interior / boundary flux records");
             if (s2 < 0 && k >= r.ngeo) return fail(t, "boundary record without normal");
             if (s2 == -4) {
                 const int q = T.qcell[r.rbase + k];

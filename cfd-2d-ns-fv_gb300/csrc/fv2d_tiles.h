@@ -10,7 +10,8 @@
 //   cells   local slots [0, ncore) core cells (device order c0 .. c0+ncore-1),
 //           [ncore, ncore+n1) ring 1, [ncore+n1, ncore+n1+n2) ring 2; halo[] lists ring 1 then ring 2
 //   records one per face the tile needs: [0, nrc) every face of a core cell (fluxes are computed for
-//           these; the first ncc join two core cells), [nrc, ngeo) boundary faces of ring-1 cells,
+//           these; the first ncc join two core cells, the first nint join two cells, the rest are
+//           boundary faces), [nrc, ngeo) boundary faces of ring-1 cells,
 //           [ngeo, nr) the other faces of ring-1 cells (gradient only).  Record block, 4-byte words:
 //             sl[nrp]   (s1 & 0xFFFF) | (s2 << 16): local slots of the face's c1 and c2 (s2 < 0: BC code)
 //             d[nrp][4] (d1x, d1y, d2x, d2y): face centre minus c1 / c2 centre (c2: ghost centre for
@@ -50,7 +51,7 @@ struct TileRec {
     long long csr = 0;     // u16 offset of the csr block
     long long halo = 0;    // int offset of the halo list
     int c0 = 0, ncore = 0, n1 = 0, n2 = 0;
-    int ncc = 0, nrc = 0, ngeo = 0, nr = 0, nrp = 0, ngp = 0;
+    int ncc = 0, nint = 0, nrc = 0, ngeo = 0, nr = 0, nrp = 0, ngp = 0;
     int noff = 0, ncsr = 0;        // u16 words: offsets part, whole block (both multiples of 8)
     int nhalo = 0;                 // ints of the halo list (n1 + n2 rounded up to 4)
 };
@@ -66,8 +67,10 @@ struct TileDesc {
     int sid;
     int ncc;               // flux records joining two core cells (the first ncc)
     int fpw;               // flux records a warp takes per grab (a multiple of 32; the batch's tuning)
+    int nint;              // flux records joining two cells (the first nint; ncc <= nint <= nrc)
+    int pad0, pad1, pad2;
 };
-static_assert(sizeof(TileDesc) == 96, "TileDesc layout");
+static_assert(sizeof(TileDesc) == 112, "TileDesc layout");
 
 struct TileLayout {
     int nc = 0;                          // cells (device order)
