@@ -317,61 +317,69 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
                     dmin[j] = 0.f; dmax[j] = 0.f;
                     tmin[j] = 3.0e38f; tmax[j] = -3.0e38f;
                 }
-                const int e0 = c_off[gI], e1 = c_off[gI + 1];
-                for (int e = e0; e < e1; e++) {
-                    const uint32_t ent = c_ent[e];
-                    const int r = (int)((ent & 0xFFFFu) >> 1), side = (int)(ent & 1u);
-                    const int so = (int)(int16_t)(ent >> 16);   // the face's other cell (or BC code)
-                    const float4 dd = r_d[r];
-                    const float d1x = dd.x, d1y = dd.y, d2x = dd.z, d2y = dd.w;
-                    float d[4];
-                    if (so >= 0) {
-                        const Q4<float> qn = cq[so];
-#pragma unroll
+                // bit 15 of the end offset: the cell has a boundary face; the others' loop has no
+                // boundary branches
+                const uint32_t o1 = c_off[gI + 1];
+                const int e0 = c_off[gI] & 0x7FFF, e1 = (int)(o1 & 0x7FFFu);
+                auto face_loop = [&](auto interior) {
+                    constexpr bool INTERIOR = decltype(interior)::value;
+                    for (int e = e0; e < e1; e++) {
+                        const uint32_t ent = c_ent[e];
+                        const int r = (int)((ent & 0xFFFFu) >> 1), side = (int)(ent & 1u);
+                        const int so = (int)(int16_t)(ent >> 16);   // the face's other cell (or BC code)
+                        const float4 dd = r_d[r];
+                        const float d1x = dd.x, d1y = dd.y, d2x = dd.z, d2y = dd.w;
+                        float d[4];
+                        if (INTERIOR || so >= 0) {
+                            const Q4<float> qn = cq[so];
+    #pragma unroll
+                            for (int j = 0; j < 4; j++) {
+                                d[j] = qn.p[j] - qc.p[j];
+                                if (squeeze) { dmin[j] = fminf(dmin[j], d[j]); dmax[j] = fmaxf(dmax[j], d[j]); }
+                            }
+                        } else if (so == -1) {
+    #pragma unroll
+                            for (int j = 0; j < 4; j++) d[j] = k.q_inf[j] - qc.p[j];
+                        } else if (so == -2 || so == -4) {
+                            float rho, u, v, P, yr;
+                            if (init_prims) { rho = k.rho_inf; u = k.u_inf; v = k.v_inf; P = k.P_inf; }
+                            else if (so == -2) tprims(qc.p, k, rho, u, v, P, yr);
+                            else {
+                                const Q4<float> qq = Qin[cbase + a.qcell[td.rbase + r]];
+                                tprims(qq.p, k, rho, u, v, P, yr);
+                            }
+                            float gq[4];
+                            if (so == -2) {   // slip wall: the cell velocity reflected (cell_gradient.cpp:43-55)
+                                const float fnx = r_nx[r], fny = r_ny[r];
+                                const float vn = u * fnx + v * fny;
+                                cons(rho, u - 2.0f * vn * fnx, v - 2.0f * vn * fny, P, k, gq);
+                            } else {          // no-slip: cell `face id`'s state, velocity negated (:62-73)
+                                cons(rho, -u, -v, P, k, gq);
+                            }
+    #pragma unroll
+                            for (int j = 0; j < 4; j++) d[j] = gq[j] - qc.p[j];
+                        } else {
+    #pragma unroll
+                            for (int j = 0; j < 4; j++) d[j] = 0.f;
+                        }
+                        // LSQ displacement c1 -> c2 (or ghost), times Q(c2) - Q(c1): for a c2-side cell the
+                        // difference above is Q(c1) - Q(c2), so the displacement's sign is flipped instead
+                        const float fx = side ? d2x - d1x : d1x - d2x, fy = side ? d2y - d1y : d1y - d2y;
+                        const float ox = side ? d2x : d1x, oy = side ? d2y : d1y;   // face centre - this cell
+    #pragma unroll
                         for (int j = 0; j < 4; j++) {
-                            d[j] = qn.p[j] - qc.p[j];
-                            if (squeeze) { dmin[j] = fminf(dmin[j], d[j]); dmax[j] = fmaxf(dmax[j], d[j]); }
-                        }
-                    } else if (so == -1) {
-#pragma unroll
-                        for (int j = 0; j < 4; j++) d[j] = k.q_inf[j] - qc.p[j];
-                    } else if (so == -2 || so == -4) {
-                        float rho, u, v, P, yr;
-                        if (init_prims) { rho = k.rho_inf; u = k.u_inf; v = k.v_inf; P = k.P_inf; }
-                        else if (so == -2) tprims(qc.p, k, rho, u, v, P, yr);
-                        else {
-                            const Q4<float> qq = Qin[cbase + a.qcell[td.rbase + r]];
-                            tprims(qq.p, k, rho, u, v, P, yr);
-                        }
-                        float gq[4];
-                        if (so == -2) {   // slip wall: the cell velocity reflected (cell_gradient.cpp:43-55)
-                            const float fnx = r_nx[r], fny = r_ny[r];
-                            const float vn = u * fnx + v * fny;
-                            cons(rho, u - 2.0f * vn * fnx, v - 2.0f * vn * fny, P, k, gq);
-                        } else {          // no-slip: cell `face id`'s state, velocity negated (:62-73)
-                            cons(rho, -u, -v, P, k, gq);
-                        }
-#pragma unroll
-                        for (int j = 0; j < 4; j++) d[j] = gq[j] - qc.p[j];
-                    } else {
-#pragma unroll
-                        for (int j = 0; j < 4; j++) d[j] = 0.f;
-                    }
-                    // LSQ displacement c1 -> c2 (or ghost), times Q(c2) - Q(c1): for a c2-side cell the
-                    // difference above is Q(c1) - Q(c2), so the displacement's sign is flipped instead
-                    const float fx = side ? d2x - d1x : d1x - d2x, fy = side ? d2y - d1y : d1y - d2y;
-                    const float ox = side ? d2x : d1x, oy = side ? d2y : d1y;   // face centre - this cell
-#pragma unroll
-                    for (int j = 0; j < 4; j++) {
-                        sx[j] += d[j] * fx;
-                        sy[j] += d[j] * fy;
-                        if (lim_prev) {
-                            const float x = gpx.p[j] * ox + gpy.p[j] * oy;
-                            tmin[j] = fminf(tmin[j], x);
-                            tmax[j] = fmaxf(tmax[j], x);
+                            sx[j] += d[j] * fx;
+                            sy[j] += d[j] * fy;
+                            if (lim_prev) {
+                                const float x = gpx.p[j] * ox + gpy.p[j] * oy;
+                                tmin[j] = fminf(tmin[j], x);
+                                tmax[j] = fmaxf(tmax[j], x);
+                            }
                         }
                     }
-                }
+                };
+                if (o1 & 0x8000u) face_loop(std::false_type{});
+                else face_loop(std::true_type{});
                 const float ixx = mom.x, iyy = mom.y, ixy = mom.z;
                 Q4<float> gx, gy;
 #pragma unroll
@@ -603,7 +611,7 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
             else { qn = a.Q[0][gid]; dprev = a.D[gid]; }
             if (STAGE == 2) lo = a.Qlo[gid];
             float r4[4] = {0.f, 0.f, 0.f, 0.f};
-            const int e0 = c_off[c], e1 = c_off[c + 1];
+            const int e0 = c_off[c] & 0x7FFF, e1 = c_off[c + 1] & 0x7FFF;
             for (int e = e0; e < e1; e++) {
                 const uint32_t ent = c_ent[e];
                 const int r = (int)((ent & 0xFFFFu) >> 1), side = (int)(ent & 1u);
@@ -690,7 +698,7 @@ __global__ void __launch_bounds__(kTileCore) k_tspec_init(const TileDesc* __rest
             const uint16_t* off = csr + d.csr;
             const uint16_t* ent = off + d.noff;
             const float* A = reinterpret_cast<const float*>(rec + d.rec + 5 * (size_t)d.nrp + 2 * (size_t)d.ngp);
-            for (int e = off[threadIdx.x]; e < off[threadIdx.x + 1]; e++) s += (fabsf(k.vn0) + k.c0) * A[ent[2 * e] >> 1];
+            for (int e = off[threadIdx.x] & 0x7FFF; e < (off[threadIdx.x + 1] & 0x7FFF); e++) s += (fabsf(k.vn0) + k.c0) * A[ent[2 * e] >> 1];
             S[d.c0 + threadIdx.x] = s;
         }
         float m = s;

@@ -110,12 +110,15 @@ bool make_tile(const DeviceLayout& L, int c0, int n, int stamp, Marks& mk, Tile&
     const int ngrad = n + n1;
     t.off.assign(ngrad + 1, 0);
     auto emit = [&](int c, int g) {
+        bool bcf = false;
         for (int i = L.inc_off[c]; i < L.inc_off[c + 1]; i++) {
             const int f = L.inc[i] >> 1, side = L.inc[i] & 1;
             const int other = side ? mk.cslot[L.fc1[f]] : (L.fc2[f] >= 0 ? mk.cslot[L.fc2[f]] : L.fc2[f]);
+            bcf = bcf || other < 0;
             t.ent.push_back((uint32_t)((mk.frec[f] << 1) | side) | ((uint32_t)(other & 0xFFFF) << 16));
         }
-        t.off[g + 1] = (uint16_t)t.ent.size();
+        // bit 15 of a cell's end offset: the cell has a boundary face
+        t.off[g + 1] = (uint16_t)(t.ent.size() | (bcf ? 0x8000u : 0u));
     };
     for (int i = 0; i < n; i++) emit(c0 + i, i);
     for (int k = 0; k < n1; k++) emit(t.ring1[k], n + k);
@@ -214,12 +217,16 @@ bool check_tile_layout(const TileLayout& T, const DeviceLayout& L, std::string& 
         }
         const uint16_t* off = T.csr.data() + r.csr;
         const uint16_t* ent = off + r.noff;   // entry e: ent[2e] (record << 1 | side), ent[2e + 1] other slot
-        if (off[0] != 0 || 2 * off[ngrad] > r.ncsr - r.noff) return fail(t, "csr offsets");
+        auto o = [&](int i) { return (int)(off[i] & 0x7FFF); };
+        if (off[0] != 0 || 2 * o(ngrad) > r.ncsr - r.noff) return fail(t, "csr offsets");
         for (int g = 0; g < ngrad; g++) {
-            if (off[g + 1] < off[g]) return fail(t, "csr offsets");
+            if (o(g + 1) < o(g)) return fail(t, "csr offsets");
             const int c = g < r.ncore ? r.c0 + g : T.halo[r.halo + g - r.ncore];
-            if (off[g + 1] - off[g] != L.inc_off[c + 1] - L.inc_off[c]) return fail(t, "csr row length");
-            for (int e = off[g]; e < off[g + 1]; e++) {
+            if (o(g + 1) - o(g) != L.inc_off[c + 1] - L.inc_off[c]) return fail(t, "csr row length");
+            bool bcf = false;
+            for (int e = o(g); e < o(g + 1); e++) bcf = bcf || (int16_t)ent[2 * e + 1] < 0;
+            if (bcf != ((off[g + 1] & 0x8000) != 0)) return fail(t, "csr boundary flag");
+            for (int e = o(g); e < o(g + 1); e++) {
                 const int rr = ent[2 * e] >> 1, side = ent[2 * e] & 1, other = (int)(int16_t)ent[2 * e + 1];
                 if (rr >= r.nr || (g < r.ncore && rr >= r.nrc)) return fail(t, "csr entry");
                 const uint32_t sl = b[rr];

@@ -19,7 +19,8 @@
 //                       record, read (and, by the flux pass, overwritten) with one 128-bit access
 //             nx[ngp] ny[ngp] A[ngp]                normal and area of records [0, ngeo)
 //           nrp = nr and ngp = ngeo rounded up to 4 (16-byte rows)
-//   csr     u16 words: off[noff] (ngrad+1 entry offsets, padded to 8 words) then 32-bit entries of
+//   csr     u16 words: off[noff] (ngrad+1 entry offsets, padded to 8 words; bit 15 of a cell's end
+//           offset off[g+1] is set when the cell has a boundary face) then 32-bit entries of
 //           every core and ring-1 cell, each cell's in ascending ORIGINAL face id (the reference's
 //           summation order), padded to 4 entries: low half (record << 1 | side), high half the local
 //           slot of the face's other cell (or its BC code, < 0) as int16, so the gradient pass needs
