@@ -18,6 +18,12 @@ H2D + step + D2H + residual norm each step; `pageable_value` with ordinary array
 (dominant kernel against the measured HBM peak, plus `fp64_pipe` against the FP64 issue peak: per
 kernel, and for the whole graph-replayed iteration in `fp64_pipe.iteration`),
 `cpu_baseline` (the oracle port on one host core), and the FP32, c4 batch and c5 serving lines.
+`roofline.fp64_pipe_frac` is the FP64 path's binding roof (the whole iteration's FP64-pipe
+instructions over the FP64 issue peak); `step_8d_frac` (FP32 lines) is the whole step's algorithmic
+bytes by the specification's formula B = N(40.67s+28) + F(9s+8 [+5s NS]) + 4(2F-Nb) per stage over
+the measured HBM peak (`_euler_geometry`: without the NS face terms).  The FP32 engine and its
+batches run one fused kernel per RK stage (`k_tstage`); the serving sample runs a persistent FP32
+batch.
 --impl reference times the reference's CPU solver step (the oracle port, a line-by-line
 restatement proven bit-identical to the reference) on the host cores: one independent replica of
 the same solve per core, a bounded sample of iterations.

@@ -270,9 +270,6 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
             for (int i = tid; i < nh; i += blockDim.x) cq[o + i] = Qin[cb + shalo[i]];
         }
         if (tid == 0) next_t = atomicAdd(a.counter + STAGE, 1);
-        // the history flags act only on an iteration's first stage (STAGE 0); the second stage's
-        // kernel, which does not read them, clears them for the next iteration
-        if (STAGE == 1 && tid == 0) { a.P[td.sid].fresh = 0; a.P[td.sid].init_prims = 0; }
         ok = mbar_wait(mb, parity) && ok;
         parity ^= 1u;
         if (__syncthreads_or(!ok)) {
@@ -553,6 +550,10 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
         if (tid == 0) { s_ctr[0] = 0; s_ctr[1] = 0; }
         if (order2) {
             if (tid == 0 && next_t < ntiles) copy_async(&tdn, a.tiles + next_t);
+            // the history flags act only on an iteration's first stage (STAGE 0); the second stage's
+            // kernel, which does not read them, clears them for the next iteration: once per solve
+            // (the tile of its first cell), in a phase long enough to cover the stores
+            if (STAGE == 1 && tid == 0 && c0 == cbase) { a.P[td.sid].fresh = 0; a.P[td.sid].init_prims = 0; }
             if (tid < ncore) grad_cell(tid);
             __syncthreads();
             if (tid == 0 && next_t < ntiles) {   // the next tile's solve parameters, if they change
@@ -571,8 +572,9 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
                     for (int r = base + lane; r < min(base + fpw, ncc); r += 32) flux_rec(r, std::true_type{});
                 }
             }
-        } else if (tid == 0 && next_t < ntiles) {
-            copy_async(&tdn, a.tiles + next_t);
+        } else {
+            if (tid == 0 && next_t < ntiles) copy_async(&tdn, a.tiles + next_t);
+            if (STAGE == 1 && tid == 0 && c0 == cbase) { a.P[td.sid].fresh = 0; a.P[td.sid].init_prims = 0; }
         }
         __syncthreads();
         if (tid == 0) {   // the next tile: its descriptor checked, its halo list copied (free now)
