@@ -375,7 +375,9 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
                         }
                     }
                 };
-                if (o1 & 0x8000u) face_loop(std::false_type{});
+                // one loop per warp: the general one if any of its cells has a boundary face (a warp
+                // running both would take the sum of the two)
+                if (__any_sync(__activemask(), (o1 & 0x8000u) != 0)) face_loop(std::false_type{});
                 else face_loop(std::true_type{});
                 const float ixx = mom.x, iyy = mom.y, ixy = mom.z;
                 Q4<float> gx, gy;
