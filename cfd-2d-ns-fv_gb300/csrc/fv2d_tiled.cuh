@@ -1,17 +1,20 @@
 // Device code of the FP32 engine: one fused kernel per SSP-RK3 stage over the tile layout of
 // fv2d_tiles.h.  Each CTA takes tiles from a counter; per tile:
-//   load    one thread arms an mbarrier and issues bulk asynchronous copies (cp.async.bulk, the
-//           TMA engine) of the tile's record block, csr block, halo list and core-cell states into
-//           shared memory; every wait on the mbarrier is bounded and reports a timeout
-//   gather  the states of the ring-1 and ring-2 cells (L2-resident neighbours of the tile)
+//   load    one thread issues bulk asynchronous copies (cp.async.bulk, the TMA engine) of the
+//           tile's record block, csr block and core-cell states into shared memory on an mbarrier
+//           (its halo list was copied, and its blocks prefetched into L2, during the previous
+//           tile's last flux pass); every wait on an mbarrier is bounded and reports a timeout
+//   gather  meanwhile, the states of the ring-1 and ring-2 cells (neighbours of the tile)
 //   grad    LSQ gradient + squeeze limiter of every core and ring-1 cell (compute_gradient,
 //           src/solver/cell_gradient.cpp:9-131; squeeze, src/solver/squeeze.cpp:9-155), each cell's
 //           sums in ascending original face id; limited gradients stay in shared memory
 //   flux    reconstruction + boundary ghosts (reconstruction.cpp:22-80), NS face terms (:86-164),
 //           Rusanov flux (rusanov.cpp:20-36) of every face of a core cell; the face's contribution
-//           V*A - F*A (res.cpp:81-89) overwrites its geometry rows in shared memory
+//           V*A - F*A (res.cpp:81-89) overwrites its displacement row in shared memory
 //   update  residual gather (res.cpp:74-109), time step (ssp_rk3.cpp:24-47) and the SSP-RK3 stage
-//           (ssp_rk3.cpp:50-77) of the core cells, in the compensated delta form of the FP32 path
+//           (ssp_rk3.cpp:50-77) of the core cells, in the compensated delta form of the FP32 path;
+//           on the last stage, per-warp spectral maxima and residual sums, folded into the solve's
+//           maximum and the tile's norm partials at the next tile's top
 // A face shared by two tiles is evaluated by both, with the same inputs and the same code, so both
 // get the same value; every per-cell sum runs in a fixed order, so results do not depend on the
 // tile schedule, and a solve gives the same bits alone and in a batch (both run these kernels).

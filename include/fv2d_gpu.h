@@ -32,7 +32,7 @@ extern "C" {
 #define FV2D_ERR_NODEV      8   /* no CUDA device / the library's kernels cannot run here       */
 
 #define FV2D_FP64 0             /* plain FP64 path, bit-exact with the reference                */
-#define FV2D_FP32 1             /* FP32 state/gradients/fluxes; FP64 LSQ matrices and norms     */
+#define FV2D_FP32 1             /* FP32 state/gradients/fluxes; LSQ terms from FP64; FP64 norms */
 
 /* Codes as read_inputs maps them (src/base/read_inputs.cpp:44-206). */
 #define FV2D_EULER 1

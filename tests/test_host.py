@@ -80,7 +80,7 @@ def test_renumbering_is_a_permutation(pkg):
     for kind, n in ((0, g.num_cells), (1, g.num_faces)):
         p = hm.permutation(kind)
         assert np.array_equal(np.sort(p), np.arange(n))
-    # Morton order keeps neighbours close: the median |new c1 - new c2| is small
+    # Hilbert order keeps neighbours close: the median |new c1 - new c2| is small
     inv = np.empty(g.num_cells, np.int64)
     inv[hm.permutation(0)] = np.arange(g.num_cells)
     inter = g.fc2 > 0
@@ -251,8 +251,10 @@ def test_tile_layout_checks(pkg, kind):
     assert t["tiles"] >= 1
     assert g.num_faces <= t["flux_records"] <= 2 * g.num_faces
     if kind == "voronoi":
-        # Morton tiles: a small share of the faces is evaluated by two tiles, and the halo rings
-        # hold about one cell per core cell
-        assert t["flux_records"] < 1.25 * g.num_faces
-        assert t["ring1"] + t["ring2"] < 1.3 * g.num_cells
+        # compact 256-cell Hilbert blocks: 1.103 flux records per face, 0.317 ring-1 and 0.319 ring-2
+        # cells per cell on this mesh (Morton blocks gave about 1.108, 0.34 and 0.36 on a similar
+        # one); the bounds leave a small margin over the measured values
+        assert t["flux_records"] < 1.115 * g.num_faces
+        assert t["ring1"] < 0.335 * g.num_cells
+        assert t["ring1"] + t["ring2"] < 0.68 * g.num_cells
     hm.close()
