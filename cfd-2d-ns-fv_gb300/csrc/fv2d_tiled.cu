@@ -170,6 +170,7 @@ public:
         int* misc = (int*)(a + omisc);
         A_.ntiles = misc; A_.counter = misc + 4; A_.err = misc + 8;
         A_.store_r = 0;
+        A_.nsmax = c.solves;
         FV2D_T(cudaMemsetAsync(arena_, 0, bytes_, stream_));
         FV2D_T(cudaStreamSynchronize(stream_));
         cells_.reset(c.cells); recw_.reset(c.recw); recs_.reset(c.recs); csr_.reset(c.csr); halo_.reset(c.halo);
@@ -294,8 +295,8 @@ public:
 
     // One stage kernel over every tile.
     int launch_stage(int st) {
-        FV2D_T(cudaMemsetAsync(A_.counter + st, 0, 4, stream_));
-        if (st == 2) FV2D_T(cudaMemsetAsync(A_.smax, 0, 4 * (size_t)caps_.solves, stream_));
+        // (the stage's tile counter was zeroed by the previous stage's kernel; the GLOBAL-dt maxima
+        // by the second stage's)
         timed(st, [&] {
             // persistent grid (CTAs that take tiles until none is left) or one CTA per tile slot
             const int gr = full_grid_ ? (int)std::max<long long>(1, hi_tiles_) : grid_;
@@ -361,6 +362,12 @@ public:
         if (e & 2) { err = "a stage kernel's wait for its tile copies timed out"; return FV2D_ERR_CUDA; }
         if (e & 4) { err = "a tile descriptor is out of range"; return FV2D_ERR_CUDA; }
         if (flags_out && nflags > 0) FV2D_T(cudaMemcpy(flags_out, A_.flags, 4 * (size_t)nflags, cudaMemcpyDeviceToHost));
+        return FV2D_OK;
+    }
+
+    // The stage kernels' tile counters zeroed (the stage sequence restarts at stage 0).
+    int reset_counters() {
+        FV2D_T(cudaMemsetAsync(A_.counter, 0, 12, stream_));
         return FV2D_OK;
     }
 
@@ -582,6 +589,7 @@ public:
         if (rc) return rc;
         rc = core_.set_history(sid_, 1, 0);   // restart: fresh face histories, primitives from the state
         if (!rc) rc = core_.spectral_init(sid_);
+        if (!rc && stage_ != 0) rc = core_.reset_counters();   // the stage sequence restarts
         if (rc) { err_ = core_.err; return rc; }
         stage_ = 0;
         return FV2D_OK;

@@ -39,7 +39,7 @@ static_assert(sizeof(TParams) % 16 == 0, "TParams is copied in 16-byte pieces");
 struct TArgs {
     const TileDesc* tiles;
     const int* ntiles;
-    int* counter;              // [3] next tile of each stage kernel (zeroed before each iteration)
+    int* counter;              // [3] next tile of each stage kernel (kernel s zeroes stage s+1's)
     TParams* P;
     const uint32_t* rec;
     const uint16_t* csr;
@@ -53,7 +53,8 @@ struct TArgs {
     float *dt, *S;
     const float *vol, *rvol;
     const float4* lsq;         // per cell: the LSQ inverse-moment terms (Ixx, Iyy, Ixy) rounded to FP32, 0
-    float* smax;               // [solves] max spectral sum (GLOBAL dt)
+    float* smax;               // [solves] max spectral sum (GLOBAL dt; zeroed by the second stage)
+    int nsmax;                 // entries of smax
     int* flags;                // [solves] non-physical state seen
     double* tpart;             // [tiles][4] residual sums of squares of the last stage (null: none)
     int* err;                  // bit 1: an mbarrier wait timed out; bit 2: a tile descriptor out of range
@@ -208,6 +209,12 @@ __global__ void __launch_bounds__(kTileCore, 3) k_tstage(TArgs a) {
         }
         s_next = next_t;
     };
+    // for the next kernel in the stream: the next stage's tile counter and, in the second stage
+    // (which does not read them), the GLOBAL-dt maxima that the last stage accumulates; stages run
+    // in order, and a restart mid-iteration zeroes the counters on the host
+    if (blockIdx.x == 0 && tid == 0) a.counter[(STAGE + 1) % 3] = 0;
+    if (STAGE == 1)
+        for (int i = blockIdx.x * blockDim.x + tid; i < a.nsmax; i += gridDim.x * blockDim.x) a.smax[i] = 0.f;
     if (tid == 0) {
         mbar_init(mb, 1);
         mbar_init(mbh, 1);
