@@ -119,7 +119,7 @@ public:
 
     ~TiledCore() {
         if (stream_) cudaStreamSynchronize(stream_);
-        if (graph_) cudaGraphExecDestroy(graph_);
+        drop_graphs();
         for (auto& p : pending_) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
         for (auto e : free_events_) cudaEventDestroy(e);
         if (arena_) cudaFree(arena_);
@@ -248,6 +248,9 @@ public:
         fill(s, hi, lo);
         FV2D_T(cudaGetLastError());
         FV2D_T(cudaMemsetAsync(A_.flags + sid, 0, 4, stream_));
+        // the tile slots' norm partials (a previous occupant's): zero until this solve's first iteration
+        if (A_.tpart && s.ntiles)
+            FV2D_T(cudaMemsetAsync(A_.tpart + 4 * (size_t)s.first_tile, 0, 32 * (size_t)s.ntiles, stream_));
         s.need_init = true;          // spectral sums before the next step
         s.image = im;
         s.active = true;
@@ -305,35 +308,55 @@ public:
             else k_tstage<2><<<gr, kTileCore, kSmTotal, stream_>>>(A_);
         });
         FV2D_T(cudaGetLastError());
-        if (st == 2 && norms_) {
-            k_tres_norm<<<caps_.solves, 256, 0, stream_>>>(srange_, A_.tpart, res2_);
-            FV2D_T(cudaGetLastError());
-        }
         return FV2D_OK;
     }
 
-    // Whole iterations as CUDA-graph replays (captured once; the graph reads the tile list from
-    // device memory, so solves join and leave without re-capture).
+    // Per-solve residual sums of squares from the last stage's per-tile partials (fixed order), on
+    // demand: the partials of a tile slot hold its last iteration's values (zero until then).
+    int reduce_norms() {
+        if (!norms_) return FV2D_OK;
+        k_tres_norm<<<caps_.solves, 256, 0, stream_>>>(srange_, A_.tpart, res2_);
+        FV2D_T(cudaGetLastError());
+        return FV2D_OK;
+    }
+
+    static constexpr int kGraphIters = 4;   // iterations per replay of the longer graph
+    void drop_graphs() {
+        for (auto& g : graph_) if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+    }
+    // Capture `iters` whole iterations as one graph.
+    int capture(int iters, cudaGraphExec_t* out) {
+        cudaGraph_t g;
+        FV2D_T(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+        int rc = FV2D_OK;
+        for (int it = 0; it < iters && !rc; it++)
+            for (int st = 0; st < 3 && !rc; st++) rc = launch_stage(st);
+        cudaError_t e = cudaStreamEndCapture(stream_, &g);
+        if (rc) return rc;
+        if (e != cudaSuccess) { err = std::string("graph capture: ") + cudaGetErrorString(e); return FV2D_ERR_CUDA; }
+        e = cudaGraphInstantiate(out, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) { *out = nullptr; err = std::string("graph instantiate: ") + cudaGetErrorString(e); return FV2D_ERR_CUDA; }
+        return FV2D_OK;
+    }
+
+    // Whole iterations as CUDA-graph replays (captured once; the graphs read the tile list from
+    // device memory, so solves join and leave without re-capture): runs of kGraphIters iterations
+    // as one replay (fewer gaps between replays), the rest one iteration per replay.
     int iterations(int n, bool graphs) {
-        for (int it = 0; it < n; it++) {
+        int it = 0;
+        while (it < n) {
+            int k = 1;
             if (!graphs || timing_) {
                 for (int st = 0; st < 3; st++) { int rc = launch_stage(st); if (rc) return rc; }
             } else {
-                if (!graph_) {
-                    cudaGraph_t g;
-                    FV2D_T(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
-                    int rc = FV2D_OK;
-                    for (int st = 0; st < 3 && !rc; st++) rc = launch_stage(st);
-                    cudaError_t e = cudaStreamEndCapture(stream_, &g);
-                    if (rc) return rc;
-                    if (e != cudaSuccess) { err = std::string("graph capture: ") + cudaGetErrorString(e); return FV2D_ERR_CUDA; }
-                    e = cudaGraphInstantiate(&graph_, g, 0);
-                    cudaGraphDestroy(g);
-                    if (e != cudaSuccess) { graph_ = nullptr; err = std::string("graph instantiate: ") + cudaGetErrorString(e); return FV2D_ERR_CUDA; }
-                }
-                FV2D_T(cudaGraphLaunch(graph_, stream_));
+                const int w = n - it >= kGraphIters ? 1 : 0;
+                k = w ? kGraphIters : 1;
+                if (!graph_[w]) { int rc = capture(k, &graph_[w]); if (rc) return rc; }
+                FV2D_T(cudaGraphLaunch(graph_[w], stream_));
             }
-            for (auto& s : solves_) if (s.active) s.iterations++;
+            for (auto& s : solves_) if (s.active) s.iterations += k;
+            it += k;
         }
         return FV2D_OK;
     }
@@ -377,7 +400,7 @@ public:
         return put_tiles(sid, true);
     }
     void set_full_grid(bool full) {
-        if (full != full_grid_ && graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
+        if (full != full_grid_) drop_graphs();
         full_grid_ = full;
     }
 
@@ -444,7 +467,7 @@ private:
         for (int k = 0; k < caps_.solves; k++)
             if (solves_[k].active) hi = std::max<long long>(hi, (long long)solves_[k].first_tile + solves_[k].ntiles);
         *cnt_pin_ = (int)hi;
-        if (full_grid_ && hi != hi_tiles_ && graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
+        if (full_grid_ && hi != hi_tiles_) drop_graphs();
         hi_tiles_ = hi;
         if (s.ntiles)
             FV2D_T(cudaMemcpyAsync((void*)(A_.tiles + s.first_tile), d, sizeof(TileDesc) * (size_t)s.ntiles,
@@ -476,7 +499,7 @@ private:
     void* arena_ = nullptr;
     int* srange_ = nullptr;
     bool keep_r_ = false, norms_ = false, timing_ = false;
-    cudaGraphExec_t graph_ = nullptr;
+    cudaGraphExec_t graph_[2] = {nullptr, nullptr};   // one iteration, kGraphIters iterations
     TileDesc* desc_pin_ = nullptr;   // page-locked mirrors: descriptors, tile ranges, tile count
     int* sr_pin_ = nullptr;
     int* cnt_pin_ = nullptr;
@@ -746,7 +769,9 @@ public:
     }
 
     int norms(int* sids, double* out, int* iters, int max, int* n) override {
-        int rc = synchronize();
+        int rc = core_.reduce_norms();
+        if (rc) { err_ = core_.err; return rc; }
+        rc = synchronize();
         std::vector<double> h(4 * (size_t)core_.caps_.solves);
         FV2D_T(cudaMemcpy(h.data(), core_.res2_, 32 * (size_t)core_.caps_.solves, cudaMemcpyDeviceToHost));
         int k = 0;
