@@ -58,3 +58,28 @@ def test_fp32_second_order_squeeze_fixed_iterations(pkg):
     out = precision.compare(g, case, drop=1e-6, max_iters=1000, check_every=100)
     print(f"squeeze @1000 it: rho_l2={out['rho_l2']:.2e} P_l2={out['P_l2']:.2e} force={out['wall_force_rel_err']:.2e}")
     assert out["rho_l2"] <= 3e-4, out["rho_l2"]
+
+
+def test_fp32_set_state_between_stages(pkg):
+    """A restart (set_state) after one stage of an iteration starts the stage sequence again: the
+    stage kernels reset each other's tile counters, so a restart mid-iteration resets them on the
+    host; the run then matches a restart made between iterations bit for bit."""
+    from conftest import bits_equal
+    g = pkg.meshgen.voronoi_bump_channel(6000, seed=1)
+    case = transonic_case(pkg)
+    src = pkg.Solver(g, case, precision=pkg.FP32)
+    src.step(3)
+    q = src.get_state()
+    src.close()
+    runs = []
+    for stages_before in (0, 1, 2):
+        s = pkg.Solver(g, case, precision=pkg.FP32)
+        if stages_before:
+            s.stage(stages_before)
+        s.set_state(q)
+        s.step(4)
+        runs.append((s.get_state(), s.residual_norm()))
+        s.close()
+    for qq, rr in runs[1:]:
+        assert bits_equal(qq, runs[0][0])
+        assert bits_equal(rr, runs[0][1])
