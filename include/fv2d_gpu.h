@@ -202,7 +202,8 @@ int fv2d_batch_add(fv2d_batch* b, const fv2d_mesh_desc* desc, const fv2d_case* c
 int fv2d_batch_add_mesh(fv2d_batch* b, const fv2d_mesh* mesh, const fv2d_case* cs, int* solve_id);
 int fv2d_batch_remove(fv2d_batch* b, int solve_id);
 int fv2d_batch_step(fv2d_batch* b, int iterations);
-/* for every active solve: id, the 4 residual L2 norms of its last iteration, iterations done   */
+/* for every active solve: id, the 4 residual L2 norms of its last iteration (summed in a fixed
+ * order, so reproducible bit for bit; meaningful once iterations > 0), iterations done         */
 int fv2d_batch_norms(fv2d_batch* b, int* solve_ids, double* norms4, int* iterations, int max, int* n);
 int fv2d_batch_get_state(fv2d_batch* b, int solve_id, double* q);
 int fv2d_batch_synchronize(fv2d_batch* b);
