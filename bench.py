@@ -439,7 +439,7 @@ def measure_batched(pkg, args, peak, peak_kind):
             "kernels": {k: {"avg_ms": round(v["avg_ms"], 4), "gbs": round(v["bytes"] / (v["avg_ms"] * 1e-3) / 1e9, 1)}
                         for k, v in per.items()},
             "finite": finite, "mesh_gen_s": round(t_gen, 1), "admit_s": round(t_add, 1),
-            "workload": "256 bump-channel Voronoi solves, cells log-uniform 2k-200k, FP32, one graph per iteration"}
+            "workload": "256 bump-channel Voronoi solves, cells log-uniform 2k-200k, FP32, graph-replayed iterations"}
 
 
 def measure_serving(pkg, args):
